@@ -1,0 +1,324 @@
+"""Benchmark of the GB300 SPH step (libsphg.so) on the 2-D dam-break workloads.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
+
+Default workload: dam_break_1m -- 1000 x 1000 particles (dx = 0.0005, a 0.5 x 0.5
+column at the left wall of the unit box, +-0.01 dx seeded jitter), h = 1.3 dx,
+weakly compressible EOS with the reference's stiffness (k = 30), rest density
+1000, artificial viscosity alpha = 0.1, gravity -9.81, dt = 1e-5, split-precision
+positions (integer cell + FP32 offset) with compensated sums.  The dam-break
+configurations name artificial viscosity as their only viscosity, so the
+reference's laminar term is off (MU = 0): with MU = 0.01 its explicit diffusion
+rate at dx = 0.0005 (MU m/rho 45/(pi h^6) (h - r), about 4e4 1/s per
+neighbour) is at the 2/dt stability limit of dt = 1e-5 and the run diverges
+(the FP64 oracle diverges the same way).
+
+One "step" is one main-loop iteration of the reference
+(integrate -> cell keys -> sort -> cell ranges -> density -> pressure -> forces).
+`value` is device time with the state resident in HBM (CUDA events on the
+launching stream, L2 flushed by a 256 MiB write between timed steps); `e2e` is
+the same run driven through the C ABI from host buffers (upload, pre-loop, K
+iterations each followed by the step-header diagnostics read back, final
+download), timed on the host around the whole sequence.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement of the reference's OpenMP path (oracle/liboracle.so, FP64, all
+threads), on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "sph-simulations_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = ("particle-steps/s on 1 GB300, batched vs plain GPU path at ≤1e-5 rel err; "
+          "p99 latency")
+UNIT = "particle-steps/s"
+BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- workloads
+def lattice_mass(rho0, h, dx):
+    """Mass that gives rho0 on a perfect square lattice of spacing dx (2-D sum of
+    the reference's poly6 kernel, 315 / (64 pi h^9) (h^2 - r^2)^3)."""
+    s = 0.0
+    m = int(math.ceil(h / dx)) + 1
+    for i in range(-m, m + 1):
+        for j in range(-m, m + 1):
+            r2 = (i * dx) ** 2 + (j * dx) ** 2
+            if r2 <= h * h:
+                s += (h * h - r2) ** 3
+    return rho0 / (315.0 / (64.0 * math.pi * h ** 9) * s)
+
+
+def dam_break(nx, ny, dx, seed, order="morton", box=(1.0, 1.0), alpha=0.1):
+    rng = np.random.default_rng(seed)
+    gx, gy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    x = (gx.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
+    y = (gy.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
+    h = 1.3 * dx
+    prm = dict(order=order, h=h, dt=1e-5, k=30.0, rho0=1000.0, mu=0.0, gx=0.0, gy=-9.81,
+               mass=lattice_mass(1000.0, h, dx), alpha=alpha, c0=math.sqrt(30.0),
+               lo=(0.0, 0.0), hi=box, periodic=0)
+    z = np.zeros(x.size)
+    return prm, x, y, z, z.copy()
+
+
+WORKLOADS = {
+    "dam_break_1m": dict(nx=1000, ny=1000, dx=0.0005, steps_config=2000, precision="split"),
+    "dam_break_12k": dict(nx=80, ny=160, dx=0.005, steps_config=1000, precision="plain"),
+}
+
+
+def make_workload(name):
+    w = WORKLOADS[name]
+    prm, x, y, vx, vy = dam_break(w["nx"], w["ny"], w["dx"], seed=0)
+    return w, prm, x, y, vx, vy
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle port)
+def cpu_baseline(prm, x, y, vx, vy, budget_s=15.0, max_steps=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    p = O.params(**prm)
+    sim = O.Sim(p, x, y, vx, vy)
+    sim.preloop()
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        sim.steps(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_steps and steps >= max_steps):
+            break
+    rate = len(x) * steps / el
+    return {"value": rate, "unit": UNIT, "cores": O.get_threads(), "kind": "port",
+            "sample": "%d particles, %d main-loop iterations after the pre-loop, FP64 CPU "
+                      "restatement of the reference's OpenMP path, %.1f s" % (len(x), steps, el)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    import sphg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w, prm, x, y, vx, vy = make_workload(args.workload)
+    n = len(x)
+    prec = sphg.SPLIT if w["precision"] == "split" else sphg.PLAIN
+    opts = sphg.options(precision=prec, track_ids=0, use_graph=1)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    # ---- device-resident timing
+    sim = sphg.Sim(sphg.params(**prm), n, opts)
+    sim.upload(x, y, vx, vy, stream=sptr)
+    sim.preloop(stream=sptr)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        sim.step(1, stream=sptr)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev[k][0].record(stream)
+        sim.step(1, stream=sptr)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = n * world * args.steps / (total_ms * 1e-3)
+
+    # ---- per-phase profile (events between the kernels of one iteration)
+    phases = np.array([sim.profile_step(stream=sptr) for _ in range(20)])
+    phase_ms = phases.mean(axis=0).tolist()
+    diag = sim.diagnostics(stream=sptr)[0]
+    launches = sim.launches_per_step() * args.steps
+    sim.close()
+
+    # ---- end to end through the C ABI from host buffers
+    sim = sphg.Sim(sphg.params(**prm), n, opts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.upload(x, y, vx, vy, stream=sptr)
+    sim.preloop(stream=sptr)
+    for k in range(args.steps):
+        sim.step(1, stream=sptr)
+        sim.diagnostics(stream=sptr)  # the per-step header (E_k, max|v|^2, N) read back
+    out = sim.download(forces=False, stream=sptr)
+    e2e_s = time.perf_counter() - t0
+    sim.close()
+    e2e = {"value": n * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(n * 16 / args.steps),
+           "d2h_bytes_per_step": int(6 * 8 + n * (2 * 8 + 4 + 4 + 4) / args.steps),
+           "wall_s": e2e_s}
+    assert np.isfinite(out["x"]).all()
+
+    hbm, src = peaks()
+    achieved = value * BYTES_PER_PARTICLE_STEP / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                "kernel": "one main-loop iteration (keys + radix sort + reorder + density + force)",
+                "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP}
+    names = ["keys", "sort", "reorder", "density", "force_integrate"]
+    tot = sum(phase_ms)
+    phases_out = {nm: {"ms": m, "share": m / tot if tot else 0.0} for nm, m in zip(names, phase_ms)}
+    dominant = max(phases_out, key=lambda k: phases_out[k]["ms"])
+
+    if rank == 0:
+        cpu = cpu_baseline(prm, x, y, vx, vy, budget_s=args.cpu_budget) if args.cpu_budget > 0 else None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered-lattice dam break (no dataset)",
+            "config": {"workload": args.workload, "particles": n, "dx": w["dx"], "h": prm["h"],
+                       "order": prm["order"], "precision": w["precision"],
+                       "physics": "k=30 rho0=1000 alpha=0.1 g=-9.81 mu=0 dt=1e-5",
+                       "steps_in_config": w["steps_config"], "replicas": "one per GPU",
+                       "l2": "flushed between timed steps (256 MiB write, outside the events)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk, "phases_ms": phases_out, "dominant_phase": dominant,
+            "diagnostics_after": {"E_k": diag[0], "max_v2": diag[1], "inside": diag[2],
+                                  "nonfinite": diag[5]},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w, prm, x, y, vx, vy = make_workload(args.workload)
+    n = len(x)
+    cpu = cpu_baseline(prm, x, y, vx, vy, budget_s=args.cpu_budget if args.cpu_budget > 0 else 15.0,
+                       max_steps=max(args.steps, 1))
+    line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded jittered-lattice dam break",
+            "config": {"workload": args.workload, "particles": n, "dx": w["dx"], "h": prm["h"],
+                       "order": prm["order"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0,
+                    help="seconds of CPU baseline sampling (0 = skip)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,158 @@
+/*
+ * sphg.h -- C ABI of the GB300 SPH step library (libsphg.so).
+ *
+ * One handle owns the device state of one or more independent 2-D SPH
+ * simulations ("instances") and runs the reference's per-step pipeline on
+ * them on one GPU:  Morton / row-major cell key -> stable key sort and cell
+ * ranges -> density -> pressure -> forces -> symplectic-Euler integration
+ * with reflecting (or periodic) walls.  Plain C types only: doubles at the
+ * boundary, device pointers as void*, a CUDA stream as an opaque void*
+ * (pass a cudaStream_t, or NULL for the legacy default stream).
+ *
+ * Every call returns an sphg_status; sphg_last_error_string() describes the
+ * most recent failure of the calling thread.
+ *
+ * Reference interfaces these calls replace (paths inside
+ * jose-pinzon0407/sph-simulations):
+ *   sphg_create / sphg_create_batch  cudaConfigure + cudaSimulationSetup
+ *                                    (app/cu_simulation_configuration.h:37-85),
+ *                                    cuCreateContainer (core/acceleration/cuContainer.cu:31-48)
+ *   sphg_upload                      cuReadContainer (core/acceleration/cuContainer.cu:50-68)
+ *   sphg_preloop                     PreLoopComputationWithCellNeighbors
+ *                                    (app/cu_simulation_configuration.h:88-164)
+ *   sphg_step                        one iteration of MaiLoopComputationWithCellNeighbors
+ *                                    (app/cu_simulation_configuration.h:166-259):
+ *                                    cuCallbackIntegrate, cuCallbackFindNeighbors,
+ *                                    cuCallbackApproximateDensitySorted, cuInvertBuffer,
+ *                                    cuKernelComputePressureSorted, cuCallbackComputeForcesSorted
+ *   sphg_download                    cuWriteContainer (core/acceleration/cuContainer.cu:70-88)
+ *   sphg_diagnostics                 cuKernelMeasurementsPerStep (core/acceleration/utils/cuUtils.cu:33-60)
+ *                                    and ComputeKineticEnergy/ComputeMaxVelocity/ParticlesInDomain
+ *                                    (core/container/MeasuringFunctions.h:5-61)
+ *   sphg_neighbor_lists              cuCallbackNeighborLists (core/acceleration/cuNeighborLists.cu:32-82)
+ *                                    and MultipassNeighborLists::AssembleNeighborList
+ *                                    (core/algorithmic/MultipassNeighborLists.h:10-14)
+ *   sphg_sort_pairs                  the thrust::sort_by_key of cuSortContainerByCellID
+ *                                    (core/acceleration/cuFindNeighbors.cu:82-100)
+ *   sphg_cell_keys                   cuSetParticlesCellIndex (core/acceleration/cuFindNeighbors.cuh:6-24)
+ */
+#ifndef SPHG_H
+#define SPHG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sphg_status {
+  SPHG_OK = 0,
+  SPHG_INVALID_ARG = 1,  /* bad size, parameter or call order */
+  SPHG_OOM = 2,          /* device allocation failed */
+  SPHG_NONFINITE = 3,    /* NaN/Inf found in an input or in the state */
+  SPHG_TIMEOUT = 4,      /* a bounded device wait gave up */
+  SPHG_CUDA_ERROR = 5,   /* a CUDA runtime call failed */
+  SPHG_CAPACITY = 6      /* a fixed capacity (cells, particles, list entries) was exceeded */
+} sphg_status;
+
+enum { SPHG_ORDER_MORTON = 0, SPHG_ORDER_ROWMAJOR = 1 };
+enum { SPHG_PRECISION_PLAIN = 0, SPHG_PRECISION_SPLIT = 1 };
+
+/* Physics and domain of one instance.  sphg_default_params() fills the
+ * reference's values: core/ConfigVariables.hpp:9-15 (H=1, TOL=1e-12,
+ * GAS_CONSTANT=30, RHO_0=25, MU=0.01), gravity -10 in y
+ * (core/compute/GenericForceComputation.tpp:141), mass 1
+ * (core/container/SoAContainer.cpp:10), and config/example.txt (dt=0.005,
+ * domain 96x48, order=rowmajor).  alpha, periodic, gx, mass != 1 are
+ * extensions; with their defaults the step is the reference's. */
+typedef struct sphg_params {
+  double h;        /* smoothing length H; also the cell size */
+  double dt;       /* time step */
+  double k;        /* GAS_CONSTANT: p = k (rho - rho0) */
+  double rho0;     /* RHO_0 */
+  double mu;       /* MU */
+  double tol;      /* TOL: the pressure term needs r > tol */
+  double gx, gy;   /* gravity */
+  double mass;     /* particle mass */
+  double alpha;    /* Monaghan artificial viscosity, 0 = off */
+  double c0;       /* sound speed of the alpha term */
+  double lo[2];    /* Domain::l_corner */
+  double hi[2];    /* Domain::h_corner */
+  int32_t order;   /* SPHG_ORDER_* */
+  int32_t periodic;/* 0 = reflecting walls (reference), 1 = periodic */
+} sphg_params;
+
+typedef struct sphg_options {
+  int32_t precision;   /* SPHG_PRECISION_PLAIN: FP32 positions;
+                          SPHG_PRECISION_SPLIT: integer cell + FP32 in-cell offset,
+                          compensated density/force sums */
+  int32_t track_ids;   /* 1: carry each particle's creation index through the sorts */
+  int32_t use_graph;   /* 1: replay each step from a captured CUDA graph */
+  int32_t reserved;
+} sphg_options;
+
+typedef struct sphg_sim sphg_sim;
+
+void sphg_default_params(sphg_params* p);
+void sphg_default_options(sphg_options* o);
+const char* sphg_last_error_string(void);
+const char* sphg_version(void);
+
+/* One instance of n particles. */
+sphg_status sphg_create(const sphg_params* p, const sphg_options* o, int64_t n, sphg_sim** out);
+/* ninst independent instances; counts[i] particles each, laid out one after the other. */
+sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t* counts,
+                              const sphg_options* o, sphg_sim** out);
+sphg_status sphg_destroy(sphg_sim* s);
+
+/* Host arrays of all instances' particles concatenated (instance order). */
+sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const double* vx,
+                        const double* vy, void* stream);
+/* FindNeighbors -> density -> pressure -> forces of the initial state. */
+sphg_status sphg_preloop(sphg_sim* s, void* stream);
+/* nsteps main-loop iterations: integrate -> FindNeighbors -> density -> pressure -> forces. */
+sphg_status sphg_step(sphg_sim* s, int64_t nsteps, void* stream);
+/* Current state in the current (cell-sorted) slot order; any pointer may be NULL.
+ * fx/fy are the forces of the current state (GenericForceComputation::ComputeForces). */
+sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double* vy,
+                          double* rho, double* fx, double* fy, int32_t* ids, void* stream);
+/* Per instance, 6 doubles: E_k, max |v|^2, particles inside the domain,
+ * sum m vx, sum m vy, non-finite count.  out has 6*ninst entries. */
+sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream);
+
+/* Debug / parity views (host copies, current slot order).  which: */
+enum {
+  SPHG_DBG_KEYS = 0,        /* int32[n]  sorted cell keys (instance-local codes) */
+  SPHG_DBG_PERM = 1,        /* int32[n]  slot before the last sort of each slot */
+  SPHG_DBG_UNSORTED_KEYS = 2,/* int32[n] keys before the last sort (previous slot order) */
+  SPHG_DBG_POS_NEXT = 3,    /* double[2n] integrated positions awaiting the next sort */
+  SPHG_DBG_VEL_NEXT = 4     /* double[2n] integrated velocities awaiting the next sort */
+};
+sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream);
+
+/* CSR neighbour lists of the current state in the reference's stencil order
+ * (self included, MultipassNeighborLists).  Call with idx == NULL to get the
+ * total in *total; offs has n+1 entries. */
+sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_t* total,
+                                void* stream);
+
+/* Runs one main-loop iteration kernel by kernel with CUDA events between the
+ * phases; ms[0..4] = keys, sort, reorder (+cell ranges), density, force+integrate
+ * (milliseconds, summed over the instances of the handle). */
+sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream);
+/* Number of kernel launches one main-loop iteration makes. */
+int32_t sphg_launches_per_step(const sphg_sim* s);
+
+/* Stand-alone kernels on caller-owned DEVICE buffers. */
+/* Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the keys.
+ * keys_out/vals_out must not alias the inputs.  Scratch is allocated by this call. */
+sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                            uint32_t* vals_out, int64_t n, int32_t bits, void* stream);
+/* Cell key of each particle (SetParticleCellIds): float positions in, int32 keys out. */
+sphg_status sphg_cell_keys(const sphg_params* p, const float* x, const float* y, int64_t n,
+                           int32_t* keys, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

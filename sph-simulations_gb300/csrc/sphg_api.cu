@@ -1,0 +1,696 @@
+// sphg_api.cu -- host side of the C ABI declared in include/sphg.h.
+//
+// A handle owns one device arena holding the state of all its instances
+// (see sphg_common.cuh for the layout), the per-instance constants computed
+// here in FP64, and optionally a captured CUDA graph of one step.  Nothing in
+// here computes physics on the host; the host only converts the caller's
+// doubles to the device representation and back.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sphg.h"
+#include "sphg_sort.cuh"
+#include "sphg_step.cuh"
+
+using sphg::InstDesc;
+using sphg::StepArgs;
+
+namespace {
+
+thread_local std::string g_err;
+
+sphg_status fail(sphg_status st, const std::string& msg) {
+  g_err = msg;
+  return st;
+}
+
+#define SPHG_CUDA(expr)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(SPHG_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+#define SPHG_TRY(expr)                   \
+  do {                                   \
+    sphg_status st_ = (expr);            \
+    if (st_ != SPHG_OK) return st_;      \
+  } while (0)
+
+int next_pow2(int n) {
+  int p = 1;
+  while (p < n) p *= 2;
+  return p;
+}
+
+uint32_t morton_host(uint32_t x, uint32_t y) {
+  uint32_t z = 0;
+  for (int b = 0; b < 16; ++b) {
+    z |= ((x >> b) & 1u) << (2 * b);
+    z |= ((y >> b) & 1u) << (2 * b + 1);
+  }
+  return z;
+}
+
+void demorton_host(uint32_t z, int& x, int& y) {
+  uint32_t a = 0, b = 0;
+  for (int i = 0; i < 16; ++i) {
+    a |= ((z >> (2 * i)) & 1u) << i;
+    b |= ((z >> (2 * i + 1)) & 1u) << i;
+  }
+  x = (int)a;
+  y = (int)b;
+}
+
+bool finite_params(const sphg_params& p) {
+  const double v[] = {p.h, p.dt, p.k, p.rho0, p.mu, p.tol, p.gx, p.gy, p.mass, p.alpha, p.c0,
+                      p.lo[0], p.lo[1], p.hi[0], p.hi[1]};
+  for (double x : v)
+    if (!std::isfinite(x)) return false;
+  return true;
+}
+
+// Per-instance constants (FP64 on the host, rounded once to FP32).  Grid as
+// MortonOrder::Initialize / RowMajorOrder::Initialize: cell size = H,
+// n = ceil(L / H), Morton pads each axis to a power of two
+// (core/alg/orders/MortonOrder.h:11-43,92-103).  Periodic boundaries (an
+// extension) use floor(L / H) cells of size L / n >= H.
+sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64_t cell_base,
+                      InstDesc& d, uint64_t& span) {
+  if (!finite_params(p)) return fail(SPHG_INVALID_ARG, "non-finite parameter");
+  if (!(p.h > 0)) return fail(SPHG_INVALID_ARG, "h must be > 0");
+  if (!(p.hi[0] > p.lo[0]) || !(p.hi[1] > p.lo[1]))
+    return fail(SPHG_INVALID_ARG, "domain must have hi > lo on both axes");
+  if (!(p.rho0 >= 0) || !(p.mass > 0) || !(p.mu >= 0) || !(p.alpha >= 0))
+    return fail(SPHG_INVALID_ARG, "rho0, mu, alpha must be >= 0 and mass > 0");
+  if (p.order != SPHG_ORDER_MORTON && p.order != SPHG_ORDER_ROWMAJOR)
+    return fail(SPHG_INVALID_ARG, "order must be SPHG_ORDER_MORTON or SPHG_ORDER_ROWMAJOR");
+  std::memset(&d, 0, sizeof(d));
+  const double L[2] = {p.hi[0] - p.lo[0], p.hi[1] - p.lo[1]};
+  int nr[2];
+  double cs[2];
+  for (int a = 0; a < 2; ++a) {
+    double n;
+    if (p.periodic) {
+      n = std::floor(L[a] / p.h);
+      if (n < 3) return fail(SPHG_INVALID_ARG, "periodic domain needs at least 3 cells of size >= h per axis");
+      cs[a] = L[a] / n;
+    } else {
+      n = std::ceil(L[a] / p.h);
+      cs[a] = p.h;
+    }
+    if (n > 65536.0) return fail(SPHG_CAPACITY, "more than 65536 cells along an axis");
+    nr[a] = (int)n;
+  }
+  d.begin = (int32_t)begin;
+  d.end = (int32_t)(begin + count);
+  d.nxr = nr[0];
+  d.nyr = nr[1];
+  d.order = p.order;
+  d.periodic = p.periodic ? 1 : 0;
+  if (p.order == SPHG_ORDER_MORTON) {
+    d.nx = next_pow2(nr[0]);
+    d.ny = next_pow2(nr[1]);
+    span = (uint64_t)morton_host((uint32_t)d.nx - 1, (uint32_t)d.ny - 1) + 1;
+  } else {
+    d.nx = nr[0];
+    d.ny = nr[1];
+    span = (uint64_t)d.nx * (uint64_t)d.ny;
+  }
+  d.cell_base = (uint32_t)cell_base;
+  d.key_span = (uint32_t)span;
+  d.lo_x = (float)p.lo[0];
+  d.lo_y = (float)p.lo[1];
+  d.hi_x = (float)p.hi[0];
+  d.hi_y = (float)p.hi[1];
+  d.cs_x = (float)cs[0];
+  d.cs_y = (float)cs[1];
+  d.inv_cs_x = (float)(1.0 / cs[0]);
+  d.inv_cs_y = (float)(1.0 / cs[1]);
+  d.Lx = (float)L[0];
+  d.Ly = (float)L[1];
+  const double h = p.h, h2 = h * h, h3 = h2 * h, h6 = h3 * h3;
+  d.h = (float)h;
+  d.inv_h2 = (float)(1.0 / h2);
+  d.h2_lo = std::nextafter((float)(h2 * (1.0 - 1.0e-6)), 0.0f);
+  d.h2_hi = std::nextafter((float)(h2 * (1.0 + 1.0e-6)), 3.0e38f);
+  d.wd = (float)(p.mass * 315.0 / (64.0 * M_PI * h3));
+  d.kp = (float)(p.mass * 1.5 * 15.0 / (M_PI * h6));
+  d.kv = (float)(p.mass * 45.0 * p.mu / (M_PI * h6));
+  d.ka = (float)(p.mass * 3.0 * 15.0 / (M_PI * h6));
+  d.k = (float)p.k;
+  d.rho0 = (float)p.rho0;
+  d.tol2 = (float)(p.tol * p.tol);
+  d.gx = (float)p.gx;
+  d.gy = (float)p.gy;
+  d.dt = (float)p.dt;
+  d.alpha_c0 = (float)(p.alpha * p.c0);
+  d.eps_h2 = (float)(0.01 * h2);
+  d.lo_xd = p.lo[0];
+  d.lo_yd = p.lo[1];
+  d.cs_xd = cs[0];
+  d.cs_yd = cs[1];
+  d.Lx_d = L[0];
+  d.Ly_d = L[1];
+  d.h2_d = h2;
+  d.mass_d = p.mass;
+  d.hi_xd = p.hi[0];
+  d.hi_yd = p.hi[1];
+  if (!std::isfinite(d.wd) || !std::isfinite(d.kp) || !std::isfinite(d.kv) || !std::isfinite(d.ka) ||
+      d.inv_h2 == 0.0f || !std::isfinite(d.inv_h2))
+    return fail(SPHG_INVALID_ARG, "h out of the FP32 range of the kernel constants");
+  return SPHG_OK;
+}
+
+// floor((x - lo)/cs) clamped exactly as the device computes it (FP64 on the host).
+int host_cell(double x, double lo, double cs, int cmax) {
+  double q = std::floor((x - lo) / cs);
+  if (!(q < (double)cmax)) return cmax;
+  if (q < 0) return 0;
+  return (int)q;
+}
+
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  template <class T>
+  T* take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+}  // namespace
+
+struct sphg_sim {
+  int ninst = 0;
+  int64_t n = 0;
+  sphg_options opt{};
+  std::vector<sphg_params> params;
+  std::vector<int64_t> counts;
+  std::vector<InstDesc> hdesc;
+  std::vector<int32_t> hbegins;
+  uint64_t total_keys = 0;
+  int key_bits = 1;
+  int diag_chunks = 1;
+  Arena arena;
+  // device buffers
+  InstDesc* ddesc = nullptr;
+  int32_t* dbegins = nullptr;
+  float2 *posA = nullptr, *posB = nullptr, *velB = nullptr, *acc = nullptr;
+  float4* velpA = nullptr;
+  float* rho = nullptr;
+  uint32_t *keyA = nullptr, *keyB = nullptr, *keyTmp = nullptr, *perm = nullptr,
+           *valTmp = nullptr, *scratch = nullptr, *flags = nullptr;
+  uint2* ranges = nullptr;
+  int32_t *idsA = nullptr, *idsB = nullptr;
+  double *diag_partials = nullptr, *diag_out = nullptr;
+  bool uploaded = false, preloop_done = false;
+  // CUDA graph of one step
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+
+  StepArgs args() const {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = n;
+    a.ninst = ninst;
+    a.track_ids = opt.track_ids;
+    a.d0 = hdesc[0];
+    a.desc = ddesc;
+    a.begins = dbegins;
+    a.posA = posA;
+    a.velpA = velpA;
+    a.rho = rho;
+    a.keyA = keyA;
+    a.ranges = ranges;
+    a.idsA = idsA;
+    a.posB = posB;
+    a.velB = velB;
+    a.keyB = keyB;
+    a.idsB = idsB;
+    a.perm = perm;
+    a.acc = acc;
+    a.flags = flags;
+    return a;
+  }
+};
+
+namespace {
+
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st) {
+  const StepArgs a = s->args();
+  const int prec = s->opt.precision;
+  SPHG_CUDA(sphg::launch_keys(a, prec, st));
+  SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
+                                   s->scratch, s->n, s->key_bits, st));
+  SPHG_CUDA(sphg::launch_reorder(a, st));
+  SPHG_CUDA(sphg::launch_density(a, prec, st));
+  SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
+  return SPHG_OK;
+}
+
+sphg_status build_graph(sphg_sim* s) {
+  if (s->gexec) return SPHG_OK;
+  if (!s->cap_stream) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  SPHG_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+  sphg_status st = enqueue_step(s, s->cap_stream);
+  cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+  if (st != SPHG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  SPHG_CUDA(e);
+  e = cudaGraphInstantiate(&s->gexec, g, 0);
+  cudaGraphDestroy(g);
+  SPHG_CUDA(e);
+  return SPHG_OK;
+}
+
+sphg_status run_steps(sphg_sim* s, int64_t k, cudaStream_t st) {
+  if (s->n == 0) return SPHG_OK;
+  if (s->opt.use_graph) {
+    SPHG_TRY(build_graph(s));
+    for (int64_t i = 0; i < k; ++i) SPHG_CUDA(cudaGraphLaunch(s->gexec, st));
+  } else {
+    for (int64_t i = 0; i < k; ++i) SPHG_TRY(enqueue_step(s, st));
+  }
+  return SPHG_OK;
+}
+
+sphg_status destroy_impl(sphg_sim* s) {
+  if (!s) return SPHG_OK;
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  if (s->arena.base) cudaFree(s->arena.base);
+  delete s;
+  return SPHG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sphg_default_params(sphg_params* p) {
+  if (!p) return;
+  p->h = 1.0;
+  p->dt = 0.005;
+  p->k = 30.0;
+  p->rho0 = 25.0;
+  p->mu = 0.01;
+  p->tol = 1.0e-12;
+  p->gx = 0.0;
+  p->gy = -10.0;
+  p->mass = 1.0;
+  p->alpha = 0.0;
+  p->c0 = std::sqrt(30.0);
+  p->lo[0] = 0.0;
+  p->lo[1] = 0.0;
+  p->hi[0] = 96.0;
+  p->hi[1] = 48.0;
+  p->order = SPHG_ORDER_ROWMAJOR;
+  p->periodic = 0;
+}
+
+void sphg_default_options(sphg_options* o) {
+  if (!o) return;
+  o->precision = SPHG_PRECISION_PLAIN;
+  o->track_ids = 1;
+  o->use_graph = 1;
+  o->reserved = 0;
+}
+
+const char* sphg_last_error_string(void) { return g_err.c_str(); }
+
+const char* sphg_version(void) { return "sphg 0.1 (sm_103a)"; }
+
+sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t* counts,
+                              const sphg_options* o, sphg_sim** out) {
+  if (!out || !p || !counts || ninst <= 0) return fail(SPHG_INVALID_ARG, "null argument or ninst <= 0");
+  *out = nullptr;
+  sphg_sim* s = new sphg_sim();
+  if (o) s->opt = *o; else sphg_default_options(&s->opt);
+  if (s->opt.precision != SPHG_PRECISION_PLAIN && s->opt.precision != SPHG_PRECISION_SPLIT) {
+    delete s;
+    return fail(SPHG_INVALID_ARG, "unknown precision mode");
+  }
+  s->ninst = ninst;
+  s->params.assign(p, p + ninst);
+  s->counts.assign(counts, counts + ninst);
+  s->hdesc.resize(ninst);
+  s->hbegins.resize(ninst);
+  int64_t begin = 0, max_n = 0;
+  uint64_t base = 0;
+  for (int i = 0; i < ninst; ++i) {
+    if (counts[i] < 0) {
+      delete s;
+      return fail(SPHG_INVALID_ARG, "negative particle count");
+    }
+    uint64_t span = 0;
+    sphg_status st = make_desc(p[i], begin, counts[i], base, s->hdesc[i], span);
+    if (st != SPHG_OK) {
+      delete s;
+      return st;
+    }
+    s->hbegins[i] = (int32_t)begin;
+    begin += counts[i];
+    base += span;
+    max_n = std::max(max_n, counts[i]);
+    if (begin >= (int64_t)0x7fffffff || base >= (uint64_t)0xfffffff0u) {
+      delete s;
+      return fail(SPHG_CAPACITY, "more than 2^31 particles or 2^32 cell keys in one handle");
+    }
+  }
+  s->n = begin;
+  s->total_keys = base;
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) < base) ++bits;
+  s->key_bits = bits;
+  s->diag_chunks = sphg::diag_chunks(max_n);
+
+  const size_t N = (size_t)std::max<int64_t>(s->n, 1);
+  // one layout function for the size probe and the real carve-up
+  auto layout = [&](Arena& A) {
+    s->ddesc = A.take<InstDesc>(ninst);
+    s->dbegins = A.take<int32_t>(ninst);
+    s->posA = A.take<float2>(N);
+    s->posB = A.take<float2>(N);
+    s->velB = A.take<float2>(N);
+    s->acc = A.take<float2>(N);
+    s->velpA = A.take<float4>(N);
+    s->rho = A.take<float>(N);
+    s->keyA = A.take<uint32_t>(N);
+    s->keyB = A.take<uint32_t>(N);
+    s->keyTmp = A.take<uint32_t>(N);
+    s->perm = A.take<uint32_t>(N);
+    s->valTmp = A.take<uint32_t>(N);
+    s->scratch = A.take<uint32_t>(sphg::sort_scratch_words(N));
+    s->flags = A.take<uint32_t>(16);
+    s->diag_partials = A.take<double>((size_t)ninst * s->diag_chunks * 6);
+    s->diag_out = A.take<double>((size_t)ninst * 6);
+    if (s->opt.track_ids) {
+      s->idsA = A.take<int32_t>(N);
+      s->idsB = A.take<int32_t>(N);
+    }
+    s->ranges = A.take<uint2>(std::max<uint64_t>(base, 1));  // last: not zero-filled
+  };
+  Arena probe;
+  layout(probe);
+  cudaError_t e = cudaMalloc(&s->arena.base, probe.used);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(SPHG_OOM, std::string("cudaMalloc of the state arena failed: ") + cudaGetErrorString(e));
+  }
+  s->arena.size = probe.used;
+  layout(s->arena);
+  sphg_status st = SPHG_OK;
+  auto chk = [&](cudaError_t err, const char* what) {
+    if (err != cudaSuccess && st == SPHG_OK) st = fail(SPHG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
+  };
+  chk(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice), "desc upload");
+  chk(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice), "begins upload");
+  // the cell-range table is never cleared again: an entry is valid only when
+  // the key stored at its start slot is the entry's own key
+  chk(cudaMemset(s->ranges, 0xff, sizeof(uint2) * std::max<uint64_t>(base, 1)), "range table init");
+  chk(cudaMemset(s->arena.base, 0, (char*)s->ranges - s->arena.base), "state init");
+  if (st != SPHG_OK) {
+    destroy_impl(s);
+    return st;
+  }
+  *out = s;
+  return SPHG_OK;
+}
+
+sphg_status sphg_create(const sphg_params* p, const sphg_options* o, int64_t n, sphg_sim** out) {
+  return sphg_create_batch(1, p, &n, o, out);
+}
+
+sphg_status sphg_destroy(sphg_sim* s) { return destroy_impl(s); }
+
+sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const double* vx,
+                        const double* vy, void* stream) {
+  if (!s || (s->n > 0 && (!x || !y || !vx || !vy))) return fail(SPHG_INVALID_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = s->n;
+  std::vector<float2> pos(n), vel(n);
+  std::vector<uint32_t> key;
+  std::vector<int32_t> ids;
+  if (s->opt.precision == SPHG_PRECISION_SPLIT) key.resize(n);
+  for (int inst = 0; inst < s->ninst; ++inst) {
+    const InstDesc& d = s->hdesc[inst];
+    const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
+    const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
+    for (int64_t i = d.begin; i < d.end; ++i) {
+      if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(vx[i]) || !std::isfinite(vy[i]))
+        return fail(SPHG_NONFINITE, "non-finite value in the uploaded state at particle " + std::to_string(i));
+      vel[i] = make_float2((float)vx[i], (float)vy[i]);
+      if (s->opt.precision == SPHG_PRECISION_SPLIT) {
+        int cx = host_cell(x[i], d.lo_xd, d.cs_xd, cmx);
+        int cy = host_cell(y[i], d.lo_yd, d.cs_yd, cmy);
+        uint32_t code = d.order == 0 ? morton_host(cx, cy) : (uint32_t)(cx + cy * d.nx);
+        key[i] = d.cell_base + code;
+        pos[i] = make_float2((float)((x[i] - d.lo_xd) - cx * d.cs_xd),
+                             (float)((y[i] - d.lo_yd) - cy * d.cs_yd));
+      } else {
+        pos[i] = make_float2((float)x[i], (float)y[i]);
+      }
+    }
+  }
+  if (n > 0) {
+    SPHG_CUDA(cudaMemcpyAsync(s->posB, pos.data(), n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    SPHG_CUDA(cudaMemcpyAsync(s->velB, vel.data(), n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    if (!key.empty())
+      SPHG_CUDA(cudaMemcpyAsync(s->keyA, key.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    if (s->opt.track_ids) {
+      ids.resize(n);
+      for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
+      SPHG_CUDA(cudaMemcpyAsync(s->idsB, ids.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
+    SPHG_CUDA(cudaStreamSynchronize(st));
+  }
+  s->uploaded = true;
+  s->preloop_done = false;
+  return SPHG_OK;
+}
+
+sphg_status sphg_preloop(sphg_sim* s, void* stream) {
+  if (!s || !s->uploaded) return fail(SPHG_INVALID_ARG, "upload a state before the pre-loop");
+  // PreLoopComputation: FindNeighbors -> density -> pressure -> forces.  The
+  // forces are consumed at once by the fused integration of the next state.
+  SPHG_TRY(run_steps(s, 1, (cudaStream_t)stream));
+  s->preloop_done = true;
+  return SPHG_OK;
+}
+
+sphg_status sphg_step(sphg_sim* s, int64_t nsteps, void* stream) {
+  if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "run sphg_preloop before sphg_step");
+  if (nsteps < 0) return fail(SPHG_INVALID_ARG, "nsteps < 0");
+  return run_steps(s, nsteps, (cudaStream_t)stream);
+}
+
+sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double* vy, double* rho,
+                          double* fx, double* fy, int32_t* ids, void* stream) {
+  if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state to download");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = s->n;
+  if (n == 0) return SPHG_OK;
+  std::vector<float2> pos(n), acc;
+  std::vector<float4> velp(n);
+  std::vector<float> r(n);
+  std::vector<uint32_t> key(n);
+  if (fx || fy) {
+    SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
+    acc.resize(n);
+    SPHG_CUDA(cudaMemcpyAsync(acc.data(), s->acc, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  }
+  SPHG_CUDA(cudaMemcpyAsync(pos.data(), s->posA, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(velp.data(), s->velpA, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(r.data(), s->rho, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(key.data(), s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  if (ids && s->opt.track_ids)
+    SPHG_CUDA(cudaMemcpyAsync(ids, s->idsA, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaStreamSynchronize(st));
+  if (ids && !s->opt.track_ids)
+    for (int64_t i = 0; i < n; ++i) ids[i] = -1;
+  for (int inst = 0; inst < s->ninst; ++inst) {
+    const InstDesc& d = s->hdesc[inst];
+    for (int64_t i = d.begin; i < d.end; ++i) {
+      double px = pos[i].x, py = pos[i].y;
+      if (s->opt.precision == SPHG_PRECISION_SPLIT) {
+        int cx, cy;
+        uint32_t code = key[i] - d.cell_base;
+        if (d.order == 0) demorton_host(code, cx, cy);
+        else { cx = (int)(code % (uint32_t)d.nx); cy = (int)(code / (uint32_t)d.nx); }
+        px = d.lo_xd + cx * d.cs_xd + px;
+        py = d.lo_yd + cy * d.cs_yd + py;
+      }
+      if (x) x[i] = px;
+      if (y) y[i] = py;
+      if (vx) vx[i] = velp[i].x;
+      if (vy) vy[i] = velp[i].y;
+      if (rho) rho[i] = r[i];
+      if (fx) fx[i] = acc[i].x;
+      if (fy) fy[i] = acc[i].y;
+    }
+  }
+  return SPHG_OK;
+}
+
+sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream) {
+  if (!s || !out) return fail(SPHG_INVALID_ARG, "null argument");
+  if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
+  cudaStream_t st = (cudaStream_t)stream;
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials,
+                                     s->diag_chunks, s->diag_out, st));
+  SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst,
+                            cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaStreamSynchronize(st));
+  return SPHG_OK;
+}
+
+sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream) {
+  if (!s || !host) return fail(SPHG_INVALID_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = s->n;
+  if (n == 0) return SPHG_OK;
+  auto local_keys = [&](const uint32_t* dev) -> sphg_status {
+    std::vector<uint32_t> k(n);
+    SPHG_CUDA(cudaMemcpyAsync(k.data(), dev, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+    int32_t* o = (int32_t*)host;
+    for (int inst = 0; inst < s->ninst; ++inst) {
+      const InstDesc& d = s->hdesc[inst];
+      for (int64_t i = d.begin; i < d.end; ++i) o[i] = (int32_t)(k[i] - d.cell_base);
+    }
+    return SPHG_OK;
+  };
+  switch (which) {
+    case SPHG_DBG_KEYS: return local_keys(s->keyA);
+    case SPHG_DBG_UNSORTED_KEYS: return local_keys(s->keyB);
+    case SPHG_DBG_PERM:
+      SPHG_CUDA(cudaMemcpyAsync(host, s->perm, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      SPHG_CUDA(cudaStreamSynchronize(st));
+      return SPHG_OK;
+    case SPHG_DBG_POS_NEXT:
+    case SPHG_DBG_VEL_NEXT: {
+      std::vector<float2> v(n);
+      std::vector<uint32_t> k;
+      const bool pos = which == SPHG_DBG_POS_NEXT;
+      SPHG_CUDA(cudaMemcpyAsync(v.data(), pos ? s->posB : s->velB, n * sizeof(float2),
+                                cudaMemcpyDeviceToHost, st));
+      if (pos && s->opt.precision == SPHG_PRECISION_SPLIT) {
+        k.resize(n);
+        SPHG_CUDA(cudaMemcpyAsync(k.data(), s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      }
+      SPHG_CUDA(cudaStreamSynchronize(st));
+      double* o = (double*)host;
+      for (int inst = 0; inst < s->ninst; ++inst) {
+        const InstDesc& d = s->hdesc[inst];
+        for (int64_t i = d.begin; i < d.end; ++i) {
+          double a = v[i].x, b = v[i].y;
+          if (!k.empty()) {
+            int cx, cy;
+            uint32_t code = k[i] - d.cell_base;
+            if (d.order == 0) demorton_host(code, cx, cy);
+            else { cx = (int)(code % (uint32_t)d.nx); cy = (int)(code / (uint32_t)d.nx); }
+            a += d.lo_xd + cx * d.cs_xd;
+            b += d.lo_yd + cy * d.cs_yd;
+          }
+          o[2 * i] = a;
+          o[2 * i + 1] = b;
+        }
+      }
+      return SPHG_OK;
+    }
+    default:
+      return fail(SPHG_INVALID_ARG, "unknown debug view");
+  }
+}
+
+sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_t* total,
+                                void* stream) {
+  if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
+  std::string err;
+  int st = sphg::lists_impl(s->args(), s->opt.precision, offs, idx, total, (cudaStream_t)stream, &err);
+  if (st != SPHG_OK) return fail((sphg_status)st, err);
+  return SPHG_OK;
+}
+
+sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
+  if (!s || !ms || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state or null output");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) SPHG_CUDA(cudaEventCreate(&ev[i]));
+  const StepArgs a = s->args();
+  const int prec = s->opt.precision;
+  sphg_status res = SPHG_OK;
+  auto run = [&]() -> sphg_status {
+    SPHG_CUDA(cudaEventRecord(ev[0], st));
+    SPHG_CUDA(sphg::launch_keys(a, prec, st));
+    SPHG_CUDA(cudaEventRecord(ev[1], st));
+    SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
+                                     s->scratch, s->n, s->key_bits, st));
+    SPHG_CUDA(cudaEventRecord(ev[2], st));
+    SPHG_CUDA(sphg::launch_reorder(a, st));
+    SPHG_CUDA(cudaEventRecord(ev[3], st));
+    SPHG_CUDA(sphg::launch_density(a, prec, st));
+    SPHG_CUDA(cudaEventRecord(ev[4], st));
+    SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
+    SPHG_CUDA(cudaEventRecord(ev[5], st));
+    SPHG_CUDA(cudaEventSynchronize(ev[5]));
+    for (int i = 0; i < 5; ++i) SPHG_CUDA(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+    return SPHG_OK;
+  };
+  res = run();
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  return res;
+}
+
+int32_t sphg_launches_per_step(const sphg_sim* s) {
+  if (!s || s->n == 0) return 0;
+  const int passes = (s->key_bits + 7) / 8;
+  return 4 + 3 * passes;
+}
+
+sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                            uint32_t* vals_out, int64_t n, int32_t bits, void* stream) {
+  if (n < 0 || bits < 1 || bits > 32) return fail(SPHG_INVALID_ARG, "n < 0 or bits outside 1..32");
+  if (n == 0) return SPHG_OK;
+  if (!keys_in || !keys_out || !vals_out) return fail(SPHG_INVALID_ARG, "null buffer");
+  if (n > 0x7fffffffLL) return fail(SPHG_CAPACITY, "n above 2^31-1");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t words = sphg::sort_scratch_words(n) + ((bits > 8) ? 2 * (size_t)n : 0);
+  uint32_t* scratch = nullptr;
+  SPHG_CUDA(cudaMallocAsync((void**)&scratch, words * sizeof(uint32_t), st));
+  uint32_t* ktmp = scratch + sphg::sort_scratch_words(n);
+  uint32_t* vtmp = ktmp + n;
+  cudaError_t e = sphg::radix_sort_pairs(keys_in, vals_in, keys_out, vals_out,
+                                         bits > 8 ? ktmp : nullptr, bits > 8 ? vtmp : nullptr,
+                                         scratch, n, bits, st);
+  cudaError_t e2 = cudaFreeAsync(scratch, st);
+  SPHG_CUDA(e);
+  SPHG_CUDA(e2);
+  return SPHG_OK;
+}
+
+sphg_status sphg_cell_keys(const sphg_params* p, const float* x, const float* y, int64_t n,
+                           int32_t* keys, void* stream) {
+  if (!p || n < 0) return fail(SPHG_INVALID_ARG, "null params or n < 0");
+  if (n == 0) return SPHG_OK;
+  if (!x || !y || !keys) return fail(SPHG_INVALID_ARG, "null buffer");
+  InstDesc d;
+  uint64_t span = 0;
+  SPHG_TRY(make_desc(*p, 0, n, 0, d, span));
+  SPHG_CUDA(sphg::launch_cell_keys_plain(d, x, y, n, keys, (cudaStream_t)stream));
+  return SPHG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// sphg_common.cuh -- device-side data layout and helpers shared by the SPH
+// step kernels.
+//
+// Layout in HBM (structure of arrays, one entry per particle slot, all
+// instances of a handle concatenated in instance order):
+//   pos    float2  position (plain) or in-cell offset (split precision)
+//   velp   float4  (vx, vy, P = p/rho^2, 1/rho)  -- written by reorder (xy) and density (zw)
+//   rho    float   density
+//   key    uint32  global cell key = instance cell_base + Morton/row-major code
+//   range  uint2   per global key: [start, end) of its particles in the sorted order
+//                  (valid only when key[start] == that key; never cleared)
+// and a second copy of pos/vel ("next" state) written by the fused
+// force+integrate kernel and consumed by the next sort.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphg {
+
+constexpr uint32_t kNoIndex = 0xFFFFFFFFu;
+
+// Per-instance constants, precomputed on the host in FP64 (sphg_api.cu).
+struct __align__(16) InstDesc {
+  int32_t begin, end;     // particle slots [begin, end)
+  uint32_t cell_base;     // first global key of this instance
+  uint32_t key_span;      // number of keys owned by this instance
+  int32_t nx, ny;         // grid extent used by the stencil bounds (Morton: padded)
+  int32_t nxr, nyr;       // real cell counts ceil(L/cs) (periodic wrap)
+  int32_t order;          // 0 Morton, 1 row-major
+  int32_t periodic;       // 0 walls, 1 periodic
+  float lo_x, lo_y, hi_x, hi_y;
+  float cs_x, cs_y, inv_cs_x, inv_cs_y;
+  float Lx, Ly;
+  float h, inv_h2;
+  float h2_lo, h2_hi;     // band around h^2 inside which the FP64 test decides
+  float wd;               // m * 315 / (64 pi h^3):  rho = wd * sum_j (1 - r^2/h^2)^3
+  float kp;               // m * 1.5 * 15 / (pi h^6):  pressure pair factor
+  float kv;               // m * 45 mu / (pi h^6):     viscosity pair factor
+  float ka;               // m * 3 * 15 / (pi h^6):    artificial-viscosity pair factor
+  float k, rho0, tol2;    // EOS stiffness, rest density, TOL^2
+  float gx, gy, dt;
+  float alpha_c0;         // alpha * c0 (0 = off)
+  float eps_h2;           // 0.01 h^2
+  double lo_xd, lo_yd, cs_xd, cs_yd, Lx_d, Ly_d, h2_d;
+  double mass_d, hi_xd, hi_yd;
+};
+
+// ---------------------------------------------------------------- Morton codes
+// Bit interleave of 16-bit coordinates: x to even bits, y to odd bits
+// (the same code as MortonOrder::MortonCode2d for coordinates < 2^16).
+__device__ __forceinline__ uint32_t part1by1(uint32_t x) {
+  x &= 0x0000ffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+__device__ __forceinline__ uint32_t compact1by1(uint32_t x) {
+  x &= 0x55555555u;
+  x = (x | (x >> 1)) & 0x33333333u;
+  x = (x | (x >> 2)) & 0x0f0f0f0fu;
+  x = (x | (x >> 4)) & 0x00ff00ffu;
+  x = (x | (x >> 8)) & 0x0000ffffu;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t local_code(const InstDesc& d, int cx, int cy) {
+  if (d.order == 0) return (part1by1((uint32_t)cy) << 1) | part1by1((uint32_t)cx);
+  return (uint32_t)cx + (uint32_t)cy * (uint32_t)d.nx;
+}
+
+__device__ __forceinline__ void decode_code(const InstDesc& d, uint32_t code, int& cx, int& cy) {
+  if (d.order == 0) {
+    cx = (int)compact1by1(code);
+    cy = (int)compact1by1(code >> 1);
+  } else {
+    cx = (int)(code % (uint32_t)d.nx);
+    cy = (int)(code / (uint32_t)d.nx);
+  }
+}
+
+// ---------------------------------------------------------------- exact cell index
+// floor((x - lo) / cs) exactly as the reference's FP64 code computes it
+// (GenericNeighborSearch.h:216-222), from an FP32 position: the FP32 quotient
+// decides unless it lies within a few ulp of a cell edge, where the FP64
+// expression decides.  Clamped to [0, cmax] (the reference clamps above only).
+__device__ __forceinline__ int cell_coord(float x, float lo, float inv_cs, double lo_d,
+                                          double cs_d, int cmax) {
+  float q = (x - lo) * inv_cs;
+  if (!(q < (float)cmax + 1.0f)) return cmax;  // also NaN
+  if (q < 0.0f) return 0;
+  float fq = floorf(q);
+  float fr = q - fq;
+  float tol = 5.0e-7f * (fabsf(x) + fabsf(lo)) * inv_cs + 1.0e-30f;
+  int c;
+  if (fr > tol && fr < 1.0f - tol) {
+    c = (int)fq;
+  } else {
+    c = (int)floor(__ddiv_rn(__dsub_rn((double)x, lo_d), cs_d));
+  }
+  return c < 0 ? 0 : (c > cmax ? cmax : c);
+}
+
+// FP64 distance test of the reference: r2 = dx*dx + dy*dy (no contraction),
+// inside when !(r2 > h2).
+static __device__ __noinline__ bool exact_inside_d(double dx, double dy, double h2_d) {
+  double r2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  return !(r2 > h2_d);
+}
+
+// ---------------------------------------------------------------- compensated sums
+struct CSum {
+  float s, c;
+  __device__ __forceinline__ CSum() : s(0.f), c(0.f) {}
+  __device__ __forceinline__ void add(float t) {  // TwoSum (Knuth), error kept in c
+    float sn = __fadd_rn(s, t);
+    float bp = __fsub_rn(sn, s);
+    float err = __fadd_rn(__fsub_rn(s, __fsub_rn(sn, bp)), __fsub_rn(t, bp));
+    s = sn;
+    c = __fadd_rn(c, err);
+  }
+  __device__ __forceinline__ float value() const { return s + c; }
+};
+
+struct PSum {
+  float s;
+  __device__ __forceinline__ PSum() : s(0.f) {}
+  __device__ __forceinline__ void add(float t) { s += t; }
+  __device__ __forceinline__ float value() const { return s; }
+};
+
+// Instance of particle slot i (binary search over instance begins; ninst is small).
+__device__ __forceinline__ int find_instance(const int32_t* __restrict__ begins, int ninst, int i) {
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(begins + mid) <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace sphg

@@ -1,0 +1,21 @@
+// sphg_sort.cuh -- host interface of the radix sort in sphg_sort.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphg {
+
+int sort_num_tiles(int64_t n);
+// 32-bit words of scratch radix_sort_pairs needs for n keys (tile histograms + digit totals).
+size_t sort_scratch_words(int64_t n);
+
+// Stable sort of (keys_in, vals_in) on the low `bits` bits; vals_in == nullptr
+// means the identity 0..n-1.  keys_tmp/vals_tmp are ping-pong buffers of n
+// entries (unused for bits <= 8).  The result lands in keys_out/vals_out.
+// No buffer may alias another.
+cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
+                             uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
+                             uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
+                             cudaStream_t stream);
+
+}  // namespace sphg

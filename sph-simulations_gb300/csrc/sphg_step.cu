@@ -1,0 +1,363 @@
+// sphg_step.cu -- the per-step SPH kernels for sm_103a.
+//
+// Step pipeline (one launch each, plus the radix sort of sphg_sort.cu):
+//   step_keys      cell key of every particle of the next state
+//                  (GenericNeighborSearch::SetParticleCellIds, GenericNeighborSearch.h:201-231)
+//   [radix sort]   stable sort of (key, slot)           (SortParticleIds, :69-76)
+//   step_reorder   gather of the state into key order + cell ranges
+//                  (SortContainer :111-191, SetCellRanges :93-108)
+//   step_density   3x3-stencil density + EOS pressure, stores p/rho^2 and 1/rho
+//                  (ApproximateDensity GenericForceComputation.tpp:35-130,
+//                   CalculatePressure :23-32, cuInvertDensity)
+//   step_force     pressure + viscosity (+ artificial viscosity) + gravity,
+//                  fused with the next step's symplectic-Euler update and walls
+//                  (ComputeForces :134-253, Integrator.cpp:7-46)
+//
+// Neighbour decisions and cell keys are the reference's FP64 decisions made
+// exactly from FP32 state: the FP32 value decides unless it lies in a thin
+// band around the threshold, where the reference's FP64 expression is
+// evaluated (sphg_common.cuh).
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "sphg_neighbor.cuh"
+#include "sphg_step.cuh"
+
+namespace sphg {
+
+constexpr int kThreads = 256;
+
+// floor(o / cs) for a split-precision offset, FP64 near integer boundaries.
+__device__ __forceinline__ int offset_cells(float o, float inv_cs, double cs_d) {
+  float q = o * inv_cs;
+  float fq = floorf(q);
+  float fr = q - fq;
+  if (fr > 1.0e-6f && fr < 1.0f - 1.0e-6f && fabsf(q) < 1.0e6f) return (int)fq;
+  if (!(fabsf(q) < 1.0e6f)) return 0;  // NaN / runaway: leave the cell, the state is flagged elsewhere
+  return (int)floor(__ddiv_rn((double)o, cs_d));
+}
+
+// ---------------------------------------------------------------- keys
+template <int PREC, bool BATCHED>
+__global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const InstDesc d = inst_of<BATCHED>(a, i);
+  float2 p = a.posB[i];
+  const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
+  const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
+  int cx, cy;
+  if (PREC == 0) {
+    cx = cell_coord(p.x, d.lo_x, d.inv_cs_x, d.lo_xd, d.cs_xd, cmx);
+    cy = cell_coord(p.y, d.lo_y, d.inv_cs_y, d.lo_yd, d.cs_yd, cmy);
+  } else {
+    int ox, oy;
+    decode_code(d, a.keyA[i] - d.cell_base, ox, oy);
+    int kx = offset_cells(p.x, d.inv_cs_x, d.cs_xd);
+    int ky = offset_cells(p.y, d.inv_cs_y, d.cs_yd);
+    cx = ox + kx;
+    cy = oy + ky;
+    if (d.periodic) {
+      p.x -= (float)kx * d.cs_x;
+      p.y -= (float)ky * d.cs_y;
+      cx = ((cx % d.nxr) + d.nxr) % d.nxr;
+      cy = ((cy % d.nyr) + d.nyr) % d.nyr;
+    } else {
+      cx = cx < 0 ? 0 : (cx > cmx ? cmx : cx);
+      cy = cy < 0 ? 0 : (cy > cmy ? cmy : cy);
+      p.x -= (float)(cx - ox) * d.cs_x;
+      p.y -= (float)(cy - oy) * d.cs_y;
+    }
+    a.posB[i] = p;
+  }
+  a.keyB[i] = d.cell_base + local_code(d, cx, cy);
+}
+
+// ---------------------------------------------------------------- reorder + cell ranges
+__global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const uint32_t src = a.perm[i];
+  const uint32_t k = a.keyA[i];
+  float2 p = a.posB[src];
+  float2 v = a.velB[src];
+  a.posA[i] = p;
+  a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
+  if (a.track_ids) a.idsA[i] = a.idsB[src];
+  uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
+  if (i == 0 || a.keyA[i - 1] != k) r[2 * (size_t)k] = (uint32_t)i;
+  if (i == a.n - 1 || a.keyA[i + 1] != k) r[2 * (size_t)k + 1] = (uint32_t)(i + 1);
+}
+
+// ---------------------------------------------------------------- density + pressure
+template <int PREC, bool BATCHED>
+__global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const InstDesc d = inst_of<BATCHED>(a, i);
+  const uint32_t key = a.keyA[i];
+  const float2 pi = a.posA[i];
+  typename std::conditional<PREC == 1, CSum, PSum>::type S;
+  int cx, cy;
+  const float inv_h2 = d.inv_h2;
+  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t, float, float, float r2) {
+    float t = fmaf(-r2, inv_h2, 1.0f);
+    S.add(t * t * t);
+  });
+  float rho, drho;
+  if constexpr (PREC == 1) {
+    rho = d.wd * S.value();
+    drho = fmaf(d.wd, S.s, -d.rho0) + d.wd * S.c;
+  } else {
+    rho = d.wd * S.value();
+    drho = rho - d.rho0;
+  }
+  const float inv = 1.0f / rho;
+  const float P = d.k * drho * inv * inv;
+  a.rho[i] = rho;
+  reinterpret_cast<float2*>(a.velpA + i)[1] = make_float2(P, inv);
+}
+
+// ---------------------------------------------------------------- forces (+ integration)
+template <int PREC, bool BATCHED, int MODE>
+__global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const InstDesc d = inst_of<BATCHED>(a, i);
+  const uint32_t key = a.keyA[i];
+  const float2 pi = a.posA[i];
+  const float4 vi = a.velpA[i];
+  typedef typename std::conditional<PREC == 1, CSum, PSum>::type Sum;
+  Sum fpx, fpy, fvx, fvy, fax, fay;
+  const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
+  const float alpha_c0 = d.alpha_c0;
+  const float4* __restrict__ velp = a.velpA;
+  int cx, cy;
+  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float dx, float dy, float r2) {
+    if (j == (uint32_t)i) return;
+    const float4 vj = __ldg(velp + j);
+    const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+    const float r = r2 * rinv;
+    const float hr = h - r;
+    if (r2 > tol2) {
+      const float s = kp * hr * hr * rinv * (vi.z + vj.z);
+      fpx.add(s * dx);
+      fpy.add(s * dy);
+    }
+    const float vm = kv * vj.w * hr;
+    fvx.add(vm * (vj.x - vi.x));
+    fvy.add(vm * (vj.y - vi.y));
+    if (alpha_c0 > 0.f && r2 > tol2) {
+      const float vr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy;
+      if (vr < 0.f) {
+        const float muij = h * vr / (r2 + d.eps_h2);
+        const float rho_bar = 0.5f * (1.0f / vi.w + 1.0f / vj.w);
+        const float pij = -alpha_c0 * muij / rho_bar;
+        const float s = d.ka * hr * hr * rinv * pij;
+        fax.add(s * dx);
+        fay.add(s * dy);
+      }
+    }
+  });
+  float ax = d.gx + fpx.value();
+  float ay = d.gy + fpy.value();
+  ax += fvx.value();
+  ay += fvy.value();
+  if (alpha_c0 > 0.f) {
+    ax += fax.value();
+    ay += fay.value();
+  }
+  if (MODE == kForceOnly) {
+    a.acc[i] = make_float2(ax, ay);
+    return;
+  }
+  // symplectic Euler (UpdateVelocities then UpdatePositions) + boundary
+  const float dt = d.dt;
+  float vx = fmaf(dt, ax, vi.x);
+  float vy = fmaf(dt, ay, vi.y);
+  float x = fmaf(dt, vx, pi.x);
+  float y = fmaf(dt, vy, pi.y);
+  if (d.periodic) {
+    if (PREC == 0) {
+      if (x >= d.hi_x) x -= d.Lx;
+      if (x < d.lo_x) x += d.Lx;
+      if (y >= d.hi_y) y -= d.Ly;
+      if (y < d.lo_y) y += d.Ly;
+    }
+    // split precision: the cell index wraps in step_keys, the offset is unchanged
+  } else {
+    float whx, wlx, why, wly;  // walls in the particle's frame
+    if (PREC == 0) {
+      whx = d.hi_x; wlx = d.lo_x; why = d.hi_y; wly = d.lo_y;
+    } else {
+      whx = d.Lx - (float)cx * d.cs_x;
+      wlx = -(float)cx * d.cs_x;
+      why = d.Ly - (float)cy * d.cs_y;
+      wly = -(float)cy * d.cs_y;
+    }
+    // Integrator::ApplyBoundaryConditions (Integrator.cpp:30-46): per axis high then low
+    if (x > whx) { x = whx; vx = -vx; }
+    if (x < wlx) { x = wlx; vx = -vx; }
+    if (y > why) { y = why; vy = -vy; }
+    if (y < wly) { y = wly; vy = -vy; }
+  }
+  a.posB[i] = make_float2(x, y);
+  a.velB[i] = make_float2(vx, vy);
+  if (a.track_ids) a.idsB[i] = a.idsA[i];
+}
+
+// ---------------------------------------------------------------- diagnostics
+constexpr int kDiagThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, int chunks,
+                                                                  double* partials) {
+  const int inst = blockIdx.y;
+  const InstDesc d = (a.ninst == 1) ? a.d0 : a.desc[inst];
+  const int64_t cnt = d.end - d.begin;
+  const int64_t per = (cnt + chunks - 1) / chunks;
+  const int64_t b = d.begin + per * blockIdx.x;
+  const int64_t e = min((int64_t)d.end, b + per);
+  double ek = 0, vmax = 0, inside = 0, px = 0, py = 0, bad = 0;
+  for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const float4 v = a.velpA[i];
+    const float2 p = a.posA[i];
+    const double vx = v.x, vy = v.y;
+    const double n2 = vx * vx + vy * vy;
+    ek += 0.5 * n2 * d.mass_d;
+    vmax = fmax(vmax, n2);
+    px += d.mass_d * vx;
+    py += d.mass_d * vy;
+    double x = p.x, y = p.y;
+    if (PREC == 1) {
+      int cx, cy;
+      decode_code(d, a.keyA[i] - d.cell_base, cx, cy);
+      x = d.lo_xd + cx * d.cs_xd + x;
+      y = d.lo_yd + cy * d.cs_yd + y;
+    }
+    const bool fin = isfinite(x) && isfinite(y) && isfinite(vx) && isfinite(vy) &&
+                     isfinite(a.rho[i]);
+    inside += (fin && !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd)) ? 1.0 : 0.0;
+    bad += fin ? 0.0 : 1.0;
+  }
+  __shared__ double sh[6][kDiagThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  ek = warp_sum(ek);
+  vmax = warp_max(vmax);
+  inside = warp_sum(inside);
+  px = warp_sum(px);
+  py = warp_sum(py);
+  bad = warp_sum(bad);
+  if (lane == 0) {
+    sh[0][w] = ek; sh[1][w] = vmax; sh[2][w] = inside; sh[3][w] = px; sh[4][w] = py; sh[5][w] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double acc = 0;
+    for (int k = 0; k < kDiagThreads / 32; ++k)
+      acc = (threadIdx.x == 1) ? fmax(acc, sh[1][k]) : acc + sh[threadIdx.x][k];
+    partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = acc;
+  }
+}
+
+__global__ void step_diag_final(int ninst, int chunks, const double* partials, double* out) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= ninst) return;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < chunks; ++c) {
+    const double* p = partials + ((size_t)inst * chunks + c) * 6;
+    for (int f = 0; f < 6; ++f) acc[f] = (f == 1) ? fmax(acc[f], p[f]) : acc[f] + p[f];
+  }
+  for (int f = 0; f < 6; ++f) out[inst * 6 + f] = acc[f];
+}
+
+// ---------------------------------------------------------------- stand-alone keys
+__global__ void cell_keys_plain(InstDesc d, const float* __restrict__ x,
+                                const float* __restrict__ y, int64_t n, int32_t* keys) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
+  const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
+  int cx = cell_coord(x[i], d.lo_x, d.inv_cs_x, d.lo_xd, d.cs_xd, cmx);
+  int cy = cell_coord(y[i], d.lo_y, d.inv_cs_y, d.lo_yd, d.cs_yd, cmy);
+  keys[i] = (int32_t)local_code(d, cx, cy);
+}
+
+// ---------------------------------------------------------------- launchers
+static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+#define SPHG_DISPATCH2(PREC_RT, BATCH_RT, KERNEL, ...)                      \
+  do {                                                                    \
+    if (PREC_RT) {                                                        \
+      if (BATCH_RT) KERNEL<1, true __VA_ARGS__><<<g, kThreads, 0, s>>>(a); \
+      else KERNEL<1, false __VA_ARGS__><<<g, kThreads, 0, s>>>(a);        \
+    } else {                                                              \
+      if (BATCH_RT) KERNEL<0, true __VA_ARGS__><<<g, kThreads, 0, s>>>(a); \
+      else KERNEL<0, false __VA_ARGS__><<<g, kThreads, 0, s>>>(a);        \
+    }                                                                     \
+  } while (0)
+
+cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(a.n, kThreads);
+  SPHG_DISPATCH2(precision, a.ninst > 1, step_keys);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  step_reorder<<<blocks_for(a.n, kThreads), kThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(a.n, kThreads);
+  SPHG_DISPATCH2(precision, a.ninst > 1, step_density);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(a.n, kThreads);
+  if (mode == kForceOnly) SPHG_DISPATCH2(precision, a.ninst > 1, step_force, , kForceOnly);
+  else SPHG_DISPATCH2(precision, a.ninst > 1, step_force, , kForceIntegrate);
+  return cudaGetLastError();
+}
+
+int diag_chunks(int64_t max_inst_n) {
+  int64_t c = (max_inst_n + 4095) / 4096;
+  if (c < 1) c = 1;
+  if (c > 256) c = 256;
+  return (int)c;
+}
+
+cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
+                               double* out, cudaStream_t s) {
+  dim3 g(chunks, a.ninst);
+  if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
+  else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
+  step_diag_final<<<blocks_for(a.ninst, 128), 128, 0, s>>>(a.ninst, chunks, partials, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const float* y, int64_t n,
+                                   int32_t* keys, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cell_keys_plain<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, x, y, n, keys);
+  return cudaGetLastError();
+}
+
+}  // namespace sphg

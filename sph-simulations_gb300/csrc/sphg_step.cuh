@@ -1,0 +1,53 @@
+// sphg_step.cuh -- launch interface of the per-step kernels (sphg_step.cu).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "sphg_common.cuh"
+
+namespace sphg {
+
+// Everything a step kernel touches.  Passed by value (kernel parameter space).
+struct StepArgs {
+  int64_t n;
+  int ninst;
+  int track_ids;
+  InstDesc d0;                 // copy of desc[0] (single-instance fast path)
+  const InstDesc* desc;        // [ninst]
+  const int32_t* begins;       // [ninst]
+  // sorted ("current") state
+  float2* posA;
+  float4* velpA;               // (vx, vy, p/rho^2, 1/rho)
+  float* rho;
+  uint32_t* keyA;              // sorted global keys
+  uint2* ranges;               // [total keys]
+  int32_t* idsA;
+  // integrated ("next") state in the current slot order
+  float2* posB;
+  float2* velB;
+  uint32_t* keyB;              // keys of the next state (sort input)
+  int32_t* idsB;
+  uint32_t* perm;              // sort output: previous slot of each new slot
+  float2* acc;                 // forces (only written on request)
+  uint32_t* flags;             // [0] non-finite count (diagnostics)
+};
+
+enum ForceMode { kForceIntegrate = 0, kForceOnly = 1 };
+
+cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s);
+cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s);
+cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s);
+// Per-instance diagnostics: partial sums per (chunk, instance) then a fixed-order
+// final sum; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx, sum m vy, nonfinite.
+cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
+                               double* out, cudaStream_t s);
+int diag_chunks(int64_t max_inst_n);
+// CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
+int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
+               cudaStream_t st, std::string* err);
+cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const float* y, int64_t n,
+                                   int32_t* keys, cudaStream_t s);
+
+}  // namespace sphg

@@ -1,0 +1,237 @@
+"""Python binding of libsphg.so (include/sphg.h) over ctypes.
+
+This is the host-side mirror of the reference's GPU driver for the SPH step
+(app/cu_simulation_configuration.h): ``Sim.preloop`` is
+PreLoopComputationWithCellNeighbors, ``Sim.step`` one iteration of
+MaiLoopComputationWithCellNeighbors, ``Sim.download`` cuWriteContainer.
+There is no CPU fallback: if libsphg.so cannot be loaded, every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsphg.so")
+
+OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY = range(7)
+ORDER = {"morton": 0, "rowmajor": 1}
+PLAIN, SPLIT = 0, 1
+DBG_KEYS, DBG_PERM, DBG_UNSORTED_KEYS, DBG_POS_NEXT, DBG_VEL_NEXT = range(5)
+
+
+class SphgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("sphg status %d: %s" % (status, msg))
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("h", ctypes.c_double), ("dt", ctypes.c_double), ("k", ctypes.c_double),
+        ("rho0", ctypes.c_double), ("mu", ctypes.c_double), ("tol", ctypes.c_double),
+        ("gx", ctypes.c_double), ("gy", ctypes.c_double), ("mass", ctypes.c_double),
+        ("alpha", ctypes.c_double), ("c0", ctypes.c_double),
+        ("lo", ctypes.c_double * 2), ("hi", ctypes.c_double * 2),
+        ("order", ctypes.c_int32), ("periodic", ctypes.c_int32),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_lp = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+def lib():
+    """Loads libsphg.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libsphg.so not built (run __graft_entry__.build()); "
+                               "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        PP = ctypes.POINTER(Params)
+        OP = ctypes.POINTER(Options)
+        SP = ctypes.c_void_p
+        L.sphg_default_params.argtypes = [PP]
+        L.sphg_default_options.argtypes = [OP]
+        L.sphg_last_error_string.restype = ctypes.c_char_p
+        L.sphg_version.restype = ctypes.c_char_p
+        L.sphg_create.argtypes = [PP, OP, ctypes.c_int64, ctypes.POINTER(SP)]
+        L.sphg_create_batch.argtypes = [ctypes.c_int32, PP, _lp, OP, ctypes.POINTER(SP)]
+        L.sphg_destroy.argtypes = [SP]
+        L.sphg_upload.argtypes = [SP, _dp, _dp, _dp, _dp, _vp]
+        L.sphg_preloop.argtypes = [SP, _vp]
+        L.sphg_step.argtypes = [SP, ctypes.c_int64, _vp]
+        L.sphg_download.argtypes = [SP] + [_dp] * 7 + [_ip, _vp]
+        L.sphg_diagnostics.argtypes = [SP, _dp, _vp]
+        L.sphg_get_debug.argtypes = [SP, ctypes.c_int32, _vp, _vp]
+        L.sphg_neighbor_lists.argtypes = [SP, _lp, _ip, _lp, _vp]
+        L.sphg_profile_step.argtypes = [SP, ctypes.POINTER(ctypes.c_float), _vp]
+        L.sphg_profile_step.restype = ctypes.c_int
+        L.sphg_launches_per_step.argtypes = [SP]
+        L.sphg_launches_per_step.restype = ctypes.c_int32
+        L.sphg_sort_pairs.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp]
+        L.sphg_cell_keys.argtypes = [PP, _vp, _vp, ctypes.c_int64, _vp, _vp]
+        for f in ("sphg_create", "sphg_create_batch", "sphg_destroy", "sphg_upload",
+                  "sphg_preloop", "sphg_step", "sphg_download", "sphg_diagnostics",
+                  "sphg_get_debug", "sphg_neighbor_lists", "sphg_sort_pairs", "sphg_cell_keys"):
+            getattr(L, f).restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != OK:
+        raise SphgError(status, lib().sphg_last_error_string().decode())
+
+
+def params(**kw):
+    """The reference's defaults (core/ConfigVariables.hpp, config/example.txt), overridable."""
+    p = Params()
+    lib().sphg_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if k in ("lo", "hi"):
+            getattr(p, k)[0], getattr(p, k)[1] = v
+        elif k == "order" and isinstance(v, str):
+            p.order = ORDER[v]
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def options(precision=PLAIN, track_ids=1, use_graph=1):
+    o = Options()
+    lib().sphg_default_options(ctypes.byref(o))
+    o.precision = precision
+    o.track_ids = track_ids
+    o.use_graph = use_graph
+    return o
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+class Sim:
+    """One handle: a single instance (params) or a batch (list of params)."""
+
+    def __init__(self, prm, n, opts=None):
+        L = lib()
+        self._h = ctypes.c_void_p()
+        if opts is None:
+            opts = options()
+        self.opts = opts
+        if isinstance(prm, (list, tuple)):
+            counts = np.ascontiguousarray(n, dtype=np.int64)
+            arr = (Params * len(prm))(*prm)
+            check(L.sphg_create_batch(len(prm), arr, _ptr(counts, _lp), ctypes.byref(opts),
+                                      ctypes.byref(self._h)))
+            self.counts = counts
+            self.n = int(counts.sum())
+            self.ninst = len(prm)
+        else:
+            check(L.sphg_create(ctypes.byref(prm), ctypes.byref(opts), int(n), ctypes.byref(self._h)))
+            self.counts = np.array([n], np.int64)
+            self.n = int(n)
+            self.ninst = 1
+
+    def upload(self, x, y, vx, vy, stream=None):
+        x, y, vx, vy = _f64(x), _f64(y), _f64(vx), _f64(vy)
+        assert len(x) == self.n
+        check(lib().sphg_upload(self._h, _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _stream(stream)))
+
+    def preloop(self, stream=None):
+        check(lib().sphg_preloop(self._h, _stream(stream)))
+
+    def step(self, k=1, stream=None):
+        check(lib().sphg_step(self._h, int(k), _stream(stream)))
+
+    def download(self, forces=True, stream=None):
+        n = self.n
+        out = {k: np.empty(n, np.float64) for k in ("x", "y", "vx", "vy", "rho")}
+        if forces:
+            out["fx"] = np.empty(n, np.float64)
+            out["fy"] = np.empty(n, np.float64)
+        ids = np.empty(n, np.int32)
+        check(lib().sphg_download(self._h, _ptr(out["x"]), _ptr(out["y"]), _ptr(out["vx"]),
+                                  _ptr(out["vy"]), _ptr(out["rho"]),
+                                  _ptr(out["fx"]) if forces else None,
+                                  _ptr(out["fy"]) if forces else None, _ptr(ids, _ip),
+                                  _stream(stream)))
+        out["ids"] = ids
+        return out
+
+    def diagnostics(self, stream=None):
+        out = np.zeros(6 * self.ninst, np.float64)
+        check(lib().sphg_diagnostics(self._h, _ptr(out), _stream(stream)))
+        return out.reshape(self.ninst, 6)
+
+    def debug(self, which, stream=None):
+        if which in (DBG_POS_NEXT, DBG_VEL_NEXT):
+            out = np.empty(2 * self.n, np.float64)
+        else:
+            out = np.empty(self.n, np.int32)
+        check(lib().sphg_get_debug(self._h, which, out.ctypes.data_as(_vp), _stream(stream)))
+        if which in (DBG_POS_NEXT, DBG_VEL_NEXT):
+            return out[0::2].copy(), out[1::2].copy()
+        return out
+
+    def neighbor_lists(self, stream=None):
+        total = ctypes.c_int64(0)
+        offs = np.empty(self.n + 1, np.int64)
+        check(lib().sphg_neighbor_lists(self._h, _ptr(offs, _lp), None, ctypes.byref(total),
+                                        _stream(stream)))
+        idx = np.empty(max(total.value, 1), np.int32)
+        check(lib().sphg_neighbor_lists(self._h, _ptr(offs, _lp), _ptr(idx, _ip),
+                                        ctypes.byref(total), _stream(stream)))
+        return offs, idx[:total.value]
+
+    def profile_step(self, stream=None):
+        """Milliseconds of keys, sort, reorder, density, force+integrate for one iteration."""
+        ms = (ctypes.c_float * 5)()
+        check(lib().sphg_profile_step(self._h, ms, _stream(stream)))
+        return list(ms)
+
+    def launches_per_step(self):
+        return int(lib().sphg_launches_per_step(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sphg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, n, bits, stream=None):
+    """Stand-alone radix sort on caller-owned device buffers (raw pointers)."""
+    check(lib().sphg_sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, int(n),
+                                int(bits), _stream(stream)))
+
+
+def cell_keys(prm, x_ptr, y_ptr, n, keys_ptr, stream=None):
+    check(lib().sphg_cell_keys(ctypes.byref(prm), x_ptr, y_ptr, int(n), keys_ptr, _stream(stream)))

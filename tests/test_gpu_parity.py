@@ -1,0 +1,371 @@
+"""Parity of the CUDA path (through the C ABI of libsphg.so) with the oracle
+and with the reference's own golden fixtures.
+
+Tolerances (the CUDA path computes in FP32, the oracle and the reference in FP64):
+  * cell keys, sorted permutation, cell membership, neighbour lists: bit-exact
+    (same FP32-representable positions in; the FP64 decision is reproduced);
+  * density: per particle |drho| / rho <= 1e-5;
+  * acceleration: max_i |da_i| / max_i |a_i| <= 1e-5 (norm-wise, per instance);
+  * integrated positions/velocities: within a few FP32 ulp of the FP64 update.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RHO_TOL = 1e-5
+ACC_TOL = 1e-5
+
+
+def _sphg():
+    import sphg
+    return sphg
+
+
+def jittered(nx, ny, dx, seed, vel=0.0):
+    rng = np.random.default_rng(seed)
+    gx, gy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    x = (gx.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
+    y = (gy.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
+    vx = rng.uniform(-vel, vel, gx.size)
+    vy = rng.uniform(-vel, vel, gx.size)
+    f = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
+    return f(x), f(y), f(vx), f(vy)
+
+
+def rel_rho(got, ref):
+    return float(np.max(np.abs(got - ref) / np.abs(ref)))
+
+
+def rel_acc(gx, gy, rx, ry):
+    scale = max(np.abs(rx).max(), np.abs(ry).max())
+    return float(max(np.abs(gx - rx).max(), np.abs(gy - ry).max()) / scale)
+
+
+def oracle_state(p, g):
+    """Oracle density/forces on the GPU's own current (sorted) state."""
+    sk = O.cell_ids(p, g["x"], g["y"])
+    s, e = O.cell_ranges(p, sk)
+    rho = O.density(p, g["x"], g["y"], sk, s, e)
+    fx, fy = O.forces(p, g["x"], g["y"], g["vx"], g["vy"], rho, sk, s, e)
+    return sk, s, e, rho, fx, fy
+
+
+# ---------------------------------------------------------------- stand-alone kernels
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_cell_keys_exact_at_cell_edges(order):
+    torch = pytest.importorskip("torch")
+    S = _sphg()
+    h = 0.0065
+    kw = dict(order=order, h=h, lo=(0, 0), hi=(1, 1))
+    rng = np.random.default_rng(5)
+    # random positions plus positions on and next to every cell edge
+    edges = np.arange(0, 155) * h
+    near = np.concatenate([edges, np.nextafter(edges.astype(np.float32), 2).astype(np.float64),
+                           np.nextafter(edges.astype(np.float32), -1).astype(np.float64)])
+    near = near[(near >= 0) & (near <= 1)]
+    x = np.concatenate([rng.uniform(0, 1, 200000), near, np.full(near.size, 0.5), [0.0, 1.0]])
+    y = np.concatenate([rng.uniform(0, 1, 200000), np.full(near.size, 0.25), near, [1.0, 0.0]])
+    x = x.astype(np.float32)
+    y = y.astype(np.float32)
+    ref = O.cell_ids(O.params(**kw), x.astype(np.float64), y.astype(np.float64))
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.from_numpy(y).cuda()
+    dk = torch.empty(len(x), dtype=torch.int32, device="cuda")
+    S.cell_keys(S.params(**kw), dx.data_ptr(), dy.data_ptr(), len(x), dk.data_ptr())
+    torch.cuda.synchronize()
+    assert (dk.cpu().numpy() == ref).all()
+
+
+@pytest.mark.parametrize("n,bits", [(0, 8), (1, 8), (2047, 8), (2048, 16), (2049, 22),
+                                    (100003, 22), (1 << 20, 25), (300000, 32)])
+def test_sort_pairs_stable(n, bits):
+    torch = pytest.importorskip("torch")
+    S = _sphg()
+    rng = np.random.default_rng(n + bits)
+    hi = (1 << bits) if bits < 32 else (1 << 32)
+    keys = rng.integers(0, min(hi, 1 << 12) if n > 1000 and bits > 16 else hi, n,
+                        dtype=np.uint64).astype(np.uint32)
+    vals = rng.permutation(n).astype(np.uint32)
+    order = np.argsort(keys, kind="stable")
+    if n == 0:
+        S.sort_pairs(0, 0, 0, 0, 0, bits)
+        return
+    ki = torch.from_numpy(keys.view(np.int32)).cuda()
+    vi = torch.from_numpy(vals.view(np.int32)).cuda()
+    ko = torch.empty_like(ki)
+    vo = torch.empty_like(vi)
+    S.sort_pairs(ki.data_ptr(), vi.data_ptr(), ko.data_ptr(), vo.data_ptr(), n, bits)
+    torch.cuda.synchronize()
+    assert (ko.cpu().numpy().view(np.uint32) == keys[order]).all()
+    assert (vo.cpu().numpy().view(np.uint32) == vals[order]).all()
+
+
+# ---------------------------------------------------------------- whole step vs reference goldens
+def test_preloop_matches_reference_cfg0(golden):
+    """12,800-particle dam-break geometry, reference physics (k=30, rho0=25, mu=0.01,
+    g=-10, m=1), h = 0.0065, Morton: keys, cell membership, density and forces
+    against the reference's own FP64 output."""
+    S = _sphg()
+    g = golden("cfg0_morton")
+    kw = dict(order="morton", h=float(g["h"]), dt=float(g["dt"]), lo=(0, 0), hi=(1, 1))
+    sim = S.Sim(S.params(**kw), len(g["x_in"]))
+    sim.upload(g["x_in"], g["y_in"], g["vx_in"], g["vy_in"])
+    sim.preloop()
+    out = sim.download()
+    keys = sim.debug(S.DBG_KEYS)
+    assert (keys == g["key"]).all()
+    # same particles in every cell as the reference's (unstable) sort
+    cells = np.unique(keys)
+    starts = np.searchsorted(keys, cells)
+    ends = np.searchsorted(keys, cells, side="right")
+    for c, b, e in zip(cells, starts, ends):
+        assert set(out["ids"][b:e]) == set(g["perm"][b:e])
+    # density and forces by particle identity
+    ref_rho = np.empty_like(g["rho"]); ref_rho[g["perm"]] = g["rho"]
+    ref_fx = np.empty_like(g["fx"]); ref_fx[g["perm"]] = g["fx"]
+    ref_fy = np.empty_like(g["fy"]); ref_fy[g["perm"]] = g["fy"]
+    assert rel_rho(out["rho"], ref_rho[out["ids"]]) <= RHO_TOL
+    assert rel_acc(out["fx"], out["fy"], ref_fx[out["ids"]], ref_fy[out["ids"]]) <= ACC_TOL
+    sim.close()
+
+
+@pytest.mark.parametrize("case", ["pair", "line3", "grid9", "wall"])
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_tiny_cases(golden, case, order):
+    S = _sphg()
+    g = golden("tiny")
+    kw = dict(order=order, h=1.0, dt=0.005, lo=(0, 0), hi=(4, 4))
+    sim = S.Sim(S.params(**kw), len(g[case + "_x_in"]))
+    sim.upload(g[case + "_x_in"], g[case + "_y_in"], g[case + "_vx_in"], g[case + "_vy_in"])
+    sim.preloop()
+    for step in (0, 1):
+        if step:
+            sim.step(1)
+        out = sim.download()
+        pre = f"{case}_{order}_s{step}_"
+        assert (sim.debug(S.DBG_KEYS) == g[pre + "key"]).all()
+        by = lambda a, ids: a[np.argsort(ids)]  # noqa: E731
+        for k in ("x", "y", "vx", "vy", "rho"):
+            ref = by(g[pre + k], g[pre + "ids"])
+            got = by(out[k], out["ids"])
+            np.testing.assert_allclose(got, ref, rtol=2e-6, atol=1e-6 * max(np.abs(ref).max(), 1e-30))
+        rx, ry = by(g[pre + "fx"], g[pre + "ids"]), by(g[pre + "fy"], g[pre + "ids"])
+        gx, gy = by(out["fx"], out["ids"]), by(out["fy"], out["ids"])
+        assert rel_acc(gx, gy, rx, ry) <= 2e-6
+    sim.close()
+
+
+def test_default_config_rowmajor(golden):
+    """The reference's own config/example.txt run (6,084 particles, H=1, rowmajor)."""
+    S = _sphg()
+    g = golden("default_rowmajor")
+    kw = dict(order="rowmajor", h=1.0, dt=0.005, lo=(0, 0), hi=(96, 48))
+    n = len(g["x_in"])
+    sim = S.Sim(S.params(**kw), n)
+    sim.upload(g["x_in"], g["y_in"], np.zeros(n), np.zeros(n))
+    sim.preloop()
+    out = sim.download()
+    assert (sim.debug(S.DBG_KEYS) == g["s0_key"]).all()
+    ref_rho = np.empty(n); ref_rho[g["s0_ids"]] = g["s0_rho"]
+    ref_fx = np.empty(n); ref_fx[g["s0_ids"]] = g["s0_fx"]
+    ref_fy = np.empty(n); ref_fy[g["s0_ids"]] = g["s0_fy"]
+    assert rel_rho(out["rho"], ref_rho[out["ids"]]) <= RHO_TOL
+    assert rel_acc(out["fx"], out["fy"], ref_fx[out["ids"]], ref_fy[out["ids"]]) <= ACC_TOL
+    sim.step(2)
+    out = sim.download()
+    ref = {k: np.empty(n) for k in ("x", "y", "vx", "vy", "rho")}
+    for k in ref:
+        ref[k][g["s2_ids"]] = g["s2_" + k]
+    for k in ("x", "y"):
+        np.testing.assert_allclose(out[k], ref[k][out["ids"]], rtol=1e-6, atol=1e-5)
+    assert rel_rho(out["rho"], ref["rho"][out["ids"]]) <= 1e-5
+    d = sim.diagnostics()[0]
+    np.testing.assert_allclose(d[0], g["s2_diag"][0], rtol=1e-4)
+    assert d[2] == g["s2_diag"][2]
+    sim.close()
+
+
+# ---------------------------------------------------------------- teacher-forced step chain
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_step_chain_teacher_forced(order):
+    """Every stage of a main-loop iteration against the oracle fed with the GPU's
+    own previous-stage output: integrate -> keys -> stable sort -> density -> forces."""
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(80, 160, dx, seed=3, vel=0.5)
+    kw = dict(order=order, h=1.3 * dx, dt=1e-5, lo=(0, 0), hi=(1, 1))
+    p = O.params(**kw)
+    sim = S.Sim(S.params(**kw), len(x))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    for it in range(3):
+        a = sim.download()
+        sk, s, e, rho, fx, fy = oracle_state(p, a)
+        assert (sim.debug(S.DBG_KEYS) == sk).all()
+        assert rel_rho(a["rho"], rho) <= RHO_TOL
+        assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+        # integration of the next state with the GPU's own forces
+        nx_, ny_ = sim.debug(S.DBG_POS_NEXT)
+        nvx, nvy = sim.debug(S.DBG_VEL_NEXT)
+        ox, oy, ovx, ovy = O.integrate(p, a["x"], a["y"], a["vx"], a["vy"], a["fx"], a["fy"])
+        for got, ref in ((nx_, ox), (ny_, oy)):
+            assert np.all(np.abs(got - ref) <= 4 * np.spacing(np.abs(ref).astype(np.float32)) + 1e-12)
+        for got, ref in ((nvx, ovx), (nvy, ovy)):
+            assert np.all(np.abs(got - ref) <= 4 * np.spacing(np.abs(ref).astype(np.float32)) + 1e-9)
+        sim.step(1)
+        # keys of the integrated state, computed from the same FP32 positions
+        assert (sim.debug(S.DBG_UNSORTED_KEYS) == O.cell_ids(p, nx_, ny_)).all()
+        perm = sim.debug(S.DBG_PERM)
+        assert (perm == O.sort_perm(O.cell_ids(p, nx_, ny_))).all()
+        b = sim.download(forces=False)
+        assert (b["x"] == nx_[perm]).all() and (b["y"] == ny_[perm]).all()
+    sim.close()
+
+
+def test_neighbor_lists_exact():
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(80, 160, dx, seed=4)
+    for order in ("morton", "rowmajor"):
+        kw = dict(order=order, h=1.3 * dx, dt=1e-5, lo=(0, 0), hi=(1, 1))
+        p = O.params(**kw)
+        sim = S.Sim(S.params(**kw), len(x))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        a = sim.download(forces=False)
+        sk = O.cell_ids(p, a["x"], a["y"])
+        s, e = O.cell_ranges(p, sk)
+        offs, idx = O.neighbor_lists(p, a["x"], a["y"], sk, s, e)
+        goffs, gidx = sim.neighbor_lists()
+        assert (goffs == offs).all() and (gidx == idx).all()
+        sim.close()
+
+
+def test_lists_golden(golden):
+    """CSR lists of the reference's MultipassNeighborLists on its own sorted state."""
+    S = _sphg()
+    g = golden("lists")
+    kw = dict(order="morton", h=float(g["h"]), dt=1e-5, lo=(0, 0), hi=(1, 1))
+    sim = S.Sim(S.params(**kw), len(g["x"]))
+    # the fixture state is already sorted by cell: the stable sort keeps its order
+    sim.upload(g["x"], g["y"], g["vx"], g["vy"])
+    sim.preloop()
+    assert (sim.debug(S.DBG_PERM) == np.arange(len(g["x"]))).all()
+    offs, idx = sim.neighbor_lists()
+    assert (offs == g["mpl_offs"]).all() and (idx == g["mpl_idx"]).all()
+    sim.close()
+
+
+def test_diagnostics_vs_oracle():
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(40, 80, dx, seed=6, vel=1.0)
+    kw = dict(order="morton", h=1.3 * dx, dt=1e-5, lo=(0, 0), hi=(1, 1))
+    sim = S.Sim(S.params(**kw), len(x))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    a = sim.download(forces=False)
+    d = sim.diagnostics()[0]
+    ref = O.diagnostics(O.params(**kw), a["x"], a["y"], a["vx"], a["vy"])
+    np.testing.assert_allclose(d[:2], ref[:2], rtol=1e-12)
+    assert d[2] == ref[2] == len(x)
+    np.testing.assert_allclose(d[3:5], ref[3:5], rtol=1e-9, atol=1e-9)
+    assert d[5] == 0
+    sim.close()
+
+
+def test_empty_and_single_particle():
+    S = _sphg()
+    kw = dict(order="morton", h=0.1, dt=1e-3, lo=(0, 0), hi=(1, 1))
+    sim = S.Sim(S.params(**kw), 0)
+    sim.upload([], [], [], [])
+    sim.preloop()
+    sim.step(3)
+    sim.close()
+    sim = S.Sim(S.params(**kw), 1)
+    sim.upload([0.5], [0.5], [0.0], [0.0])
+    sim.preloop()
+    out = sim.download()
+    p = O.params(**kw)
+    assert abs(out["fy"][0] - (-10.0)) < 1e-6  # gravity only
+    wd = 315.0 / (64 * np.pi * 0.1 ** 3)
+    assert abs(out["rho"][0] - wd) / wd < 1e-6  # self term only
+    sim.step(10)
+    out = sim.download()
+    oy, ovy = 0.5, 0.0
+    for _ in range(10):  # ten main-loop iterations, each one integration
+        ovy += p.dt * -10.0
+        oy += p.dt * ovy
+    assert abs(out["y"][0] - oy) < 1e-6 and abs(out["vy"][0] - ovy) < 1e-6
+    sim.close()
+
+
+def test_invalid_arguments_fail_loudly():
+    S = _sphg()
+    with pytest.raises(S.SphgError):
+        S.Sim(S.params(h=-1.0), 10)
+    with pytest.raises(S.SphgError):
+        S.Sim(S.params(hi=(0.0, 1.0), lo=(0.0, 0.0)), 10)
+    sim = S.Sim(S.params(h=0.1, lo=(0, 0), hi=(1, 1)), 2)
+    with pytest.raises(S.SphgError):
+        sim.step(1)  # before the pre-loop
+    with pytest.raises(S.SphgError) as ei:
+        sim.upload([0.1, np.nan], [0.1, 0.2], [0, 0], [0, 0])
+    assert ei.value.status == S.NONFINITE
+    sim.close()
+
+
+# ---------------------------------------------------------------- split-precision positions
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_split_precision_step_chain(order):
+    """Integer cell + FP32 offset positions with compensated sums: density and
+    forces against the oracle on the reconstructed positions, keys exact."""
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(80, 160, dx, seed=7, vel=0.5)
+    kw = dict(order=order, h=1.3 * dx, dt=1e-5, lo=(0, 0), hi=(1, 1))
+    p = O.params(**kw)
+    sim = S.Sim(S.params(**kw), len(x), S.options(precision=S.SPLIT))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    for it in range(4):
+        a = sim.download()
+        # reconstructed positions within float rounding of the uploaded ones at step 0
+        if it == 0:
+            ix = np.argsort(a["ids"])
+            assert np.max(np.abs(a["x"][ix] - x)) < 1e-9 and np.max(np.abs(a["y"][ix] - y)) < 1e-9
+        sk, s, e, rho, fx, fy = oracle_state(p, a)
+        assert (sim.debug(S.DBG_KEYS) == sk).all()
+        assert rel_rho(a["rho"], rho) <= RHO_TOL
+        assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+        nx_, ny_ = sim.debug(S.DBG_POS_NEXT)
+        ox, oy, ovx, ovy = O.integrate(p, a["x"], a["y"], a["vx"], a["vy"], a["fx"], a["fy"])
+        assert np.max(np.abs(nx_ - ox)) < 1e-9 and np.max(np.abs(ny_ - oy)) < 1e-9
+        sim.step(1)
+    sim.close()
+
+
+def test_split_and_plain_agree_over_many_steps():
+    """Both position representations follow the same trajectory (FP32 noise only)."""
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(40, 80, dx, seed=8)
+    kw = dict(order="morton", h=1.3 * dx, dt=1e-5, k=30.0, rho0=1000.0, gy=-9.81,
+              mass=1.0e-4, alpha=0.1, lo=(0, 0), hi=(1, 1))
+    out = []
+    for prec in (S.PLAIN, S.SPLIT):
+        sim = S.Sim(S.params(**kw), len(x), S.options(precision=prec))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        sim.step(200)
+        a = sim.download(forces=False)
+        ix = np.argsort(a["ids"])
+        out.append((a["x"][ix], a["y"][ix], sim.diagnostics()[0]))
+        sim.close()
+    # 200 steps of FP32 rounding in different position representations: << dx = 5e-3
+    assert np.max(np.abs(out[0][0] - out[1][0])) < 1e-5
+    assert np.max(np.abs(out[0][1] - out[1][1])) < 1e-5
+    assert out[1][2][2] == len(x) and out[1][2][5] == 0
