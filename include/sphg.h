@@ -148,6 +148,22 @@ int32_t sphg_launches_per_step(const sphg_sim* s);
  * keys_out/vals_out must not alias the inputs.  Scratch is allocated by this call. */
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                             uint32_t* vals_out, int64_t n, int32_t bits, void* stream);
+/* Largest n sphg_sort_pairs_noalloc accepts. */
+#define SPHG_SORT_NOALLOC_MAX_PAIRS 262144
+/* sphg_sort_pairs for callers that cannot allocate device memory when they
+ * sort (allocation-free graph capture, fixed-budget allocators, hosts that
+ * forbid cudaMalloc).  No counterpart in the reference.  Same arguments and
+ * result as sphg_sort_pairs, but its scratch is a fixed device array inside
+ * the library (2,229,248 bytes, held on every GPU that loads the library until
+ * the process exits), so n must be <= SPHG_SORT_NOALLOC_MAX_PAIRS
+ * (SPHG_CAPACITY otherwise).  It calls no cudaMalloc/cudaFree.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (different streams, or different host
+ * threads on one device) race and corrupt each other's results. */
+sphg_status sphg_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in,
+                                    uint32_t* keys_out, uint32_t* vals_out, int64_t n,
+                                    int32_t bits, void* stream);
 /* Cell key of each particle (SetParticleCellIds): float positions in, int32 keys out. */
 sphg_status sphg_cell_keys(const sphg_params* p, const float* x, const float* y, int64_t n,
                            int32_t* keys, void* stream);

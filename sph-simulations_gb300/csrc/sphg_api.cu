@@ -189,6 +189,10 @@ struct Arena {
 
 }  // namespace
 
+namespace sphg {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace sphg
+
 struct sphg_sim {
   int ninst = 0;
   int64_t n = 0;

@@ -47,6 +47,8 @@ int diag_chunks(int64_t max_inst_n);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
                cudaStream_t st, std::string* err);
+// Records the message returned by sphg_last_error_string() (sphg_api.cu).
+void set_last_error(const std::string& msg);
 cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const float* y, int64_t n,
                                    int32_t* keys, cudaStream_t s);
 
