@@ -88,7 +88,9 @@ typedef struct sphg_options {
                           compensated density/force sums */
   int32_t track_ids;   /* 1: carry each particle's creation index through the sorts */
   int32_t use_graph;   /* 1: replay each step from a captured CUDA graph */
-  int32_t reserved;
+  int32_t tile_bits;   /* density/force cell tiles of 2^b x 2^b cells staged in shared memory:
+                          0 = default (off), 3..5 = that b (every instance in Morton order),
+                          -1 = off (one thread per particle, L1-cached global loads) */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;
@@ -124,7 +126,7 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream);
 enum {
   SPHG_DBG_KEYS = 0,        /* int32[n]  sorted cell keys (instance-local codes) */
   SPHG_DBG_PERM = 1,        /* int32[n]  slot before the last sort of each slot */
-  SPHG_DBG_UNSORTED_KEYS = 2,/* int32[n] keys before the last sort (previous slot order) */
+  SPHG_DBG_UNSORTED_KEYS = 2,/* int32[n] keys of the integrated state awaiting the next sort */
   SPHG_DBG_POS_NEXT = 3,    /* double[2n] integrated positions awaiting the next sort */
   SPHG_DBG_VEL_NEXT = 4     /* double[2n] integrated velocities awaiting the next sort */
 };

@@ -161,6 +161,8 @@ sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64
   d.mass_d = p.mass;
   d.hi_xd = p.hi[0];
   d.hi_yd = p.hi[1];
+  d.half_Lx_d = 0.5 * L[0];
+  d.half_Ly_d = 0.5 * L[1];
   if (!std::isfinite(d.wd) || !std::isfinite(d.kp) || !std::isfinite(d.kv) || !std::isfinite(d.ka) ||
       d.inv_h2 == 0.0f || !std::isfinite(d.inv_h2))
     return fail(SPHG_INVALID_ARG, "h out of the FP32 range of the kernel constants");
@@ -213,9 +215,14 @@ struct sphg_sim {
   float* rho = nullptr;
   uint32_t *keyA = nullptr, *keyB = nullptr, *keyTmp = nullptr, *perm = nullptr,
            *valTmp = nullptr, *scratch = nullptr, *flags = nullptr;
-  uint2* ranges = nullptr;
+  uint4* ranges = nullptr;
   int32_t *idsA = nullptr, *idsB = nullptr;
   double *diag_partials = nullptr, *diag_out = nullptr;
+  uint2* tile_ranges = nullptr;
+  uint32_t* tile_list = nullptr;
+  uint32_t *nbr = nullptr, *ncount = nullptr;
+  int nbr_slots = 0;
+  int tile_bits = 0, tile_cap = 0, tile_grid = 0;
   bool uploaded = false, preloop_done = false;
   // CUDA graph of one step
   cudaStream_t cap_stream = nullptr;
@@ -235,6 +242,7 @@ struct sphg_sim {
     a.rho = rho;
     a.keyA = keyA;
     a.ranges = ranges;
+    a.epoch = flags + 2;
     a.idsA = idsA;
     a.posB = posB;
     a.velB = velB;
@@ -243,21 +251,38 @@ struct sphg_sim {
     a.perm = perm;
     a.acc = acc;
     a.flags = flags;
+    a.tile_bits = tile_bits;
+    a.tile_cap = tile_cap;
+    a.tile_grid = tile_grid;
+    a.tile_ranges = tile_ranges;
+    a.tile_list = tile_list;
+    a.tile_count = flags + 1;
+    a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
+    a.ncount = ncount;
+    a.nbr_slots = nbr_slots;
     return a;
   }
 };
 
 namespace {
 
-sphg_status enqueue_step(sphg_sim* s, cudaStream_t st) {
+// One main-loop iteration.  The force kernel writes the keys of the integrated
+// state, so the key pass only runs on the first iteration after an upload.
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
-  SPHG_CUDA(sphg::launch_keys(a, prec, st));
+  if (first) SPHG_CUDA(sphg::launch_keys(a, prec, st));
   SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                   s->scratch, s->n, s->key_bits, st));
+                                   s->scratch, s->n, s->key_bits, st, s->flags + 2));
+  if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
-  SPHG_CUDA(sphg::launch_density(a, prec, st));
-  SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
+  if (s->tile_bits) {
+    SPHG_CUDA(sphg::launch_tiled(a, prec, false, st));
+    SPHG_CUDA(sphg::launch_tiled(a, prec, true, st));
+  } else {
+    SPHG_CUDA(sphg::launch_density(a, prec, st));
+    SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
+  }
   return SPHG_OK;
 }
 
@@ -279,8 +304,12 @@ sphg_status build_graph(sphg_sim* s) {
   return SPHG_OK;
 }
 
-sphg_status run_steps(sphg_sim* s, int64_t k, cudaStream_t st) {
+sphg_status run_steps(sphg_sim* s, int64_t k, cudaStream_t st, bool first = false) {
   if (s->n == 0) return SPHG_OK;
+  if (first) {
+    SPHG_TRY(enqueue_step(s, st, true));
+    --k;
+  }
   if (s->opt.use_graph) {
     SPHG_TRY(build_graph(s));
     for (int64_t i = 0; i < k; ++i) SPHG_CUDA(cudaGraphLaunch(s->gexec, st));
@@ -329,7 +358,7 @@ void sphg_default_options(sphg_options* o) {
   o->precision = SPHG_PRECISION_PLAIN;
   o->track_ids = 1;
   o->use_graph = 1;
-  o->reserved = 0;
+  o->tile_bits = 0;
 }
 
 const char* sphg_last_error_string(void) { return g_err.c_str(); }
@@ -351,6 +380,17 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   s->counts.assign(counts, counts + ninst);
   s->hdesc.resize(ninst);
   s->hbegins.resize(ninst);
+  bool all_morton = true;
+  for (int i = 0; i < ninst; ++i) all_morton = all_morton && p[i].order == SPHG_ORDER_MORTON;
+  int tb = s->opt.tile_bits;
+  if (tb == 0) tb = -1;  // default: one thread per particle (faster than the tiles at these densities)
+  if (tb > 0 && (!all_morton || tb < 3 || tb > 5)) {
+    delete s;
+    return fail(SPHG_INVALID_ARG, "cell tiles need Morton order on every instance and tile_bits in 3..5");
+  }
+  s->tile_bits = tb > 0 ? tb : 0;
+  // instances start on a tile boundary of the key space so no tile spans two instances
+  const uint64_t key_align = s->tile_bits ? ((uint64_t)1 << (2 * 5)) : 1;
   int64_t begin = 0, max_n = 0;
   uint64_t base = 0;
   for (int i = 0; i < ninst; ++i) {
@@ -366,7 +406,7 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
     }
     s->hbegins[i] = (int32_t)begin;
     begin += counts[i];
-    base += span;
+    base += (span + key_align - 1) / key_align * key_align;
     max_n = std::max(max_n, counts[i]);
     if (begin >= (int64_t)0x7fffffff || base >= (uint64_t)0xfffffff0u) {
       delete s;
@@ -381,6 +421,9 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   s->diag_chunks = sphg::diag_chunks(max_n);
 
   const size_t N = (size_t)std::max<int64_t>(s->n, 1);
+  // per-particle neighbour slots filled by the density pass and read by the
+  // force pass (indices are packed as j << 5, so only below 2^27 particles)
+  s->nbr_slots = (s->n < ((int64_t)1 << 27)) ? 12 : 0;
   // one layout function for the size probe and the real carve-up
   auto layout = [&](Arena& A) {
     s->ddesc = A.take<InstDesc>(ninst);
@@ -404,8 +447,22 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
       s->idsA = A.take<int32_t>(N);
       s->idsB = A.take<int32_t>(N);
     }
-    s->ranges = A.take<uint2>(std::max<uint64_t>(base, 1));  // last: not zero-filled
+    if (s->nbr_slots) {
+      s->nbr = A.take<uint32_t>(N * (size_t)s->nbr_slots);
+      s->ncount = A.take<uint32_t>(N);
+    }
+    if (s->tile_bits) {
+      s->tile_ranges = A.take<uint2>((base >> (2 * s->tile_bits)) + 1);
+      s->tile_list = A.take<uint32_t>(std::min<uint64_t>(N, (base >> (2 * s->tile_bits)) + 1));
+    }
+    s->ranges = A.take<uint4>(std::max<uint64_t>(base, 1));
   };
+  if (s->tile_bits) {
+    const int fw = (1 << s->tile_bits) + 2;
+    s->tile_cap = (3 * fw * fw + 127) / 128 * 128;
+    const uint64_t max_tiles = std::min<uint64_t>(N, (base >> (2 * s->tile_bits)) + 1);
+    s->tile_grid = (int)std::min<uint64_t>(max_tiles, 4096);
+  }
   Arena probe;
   layout(probe);
   cudaError_t e = cudaMalloc(&s->arena.base, probe.used);
@@ -421,10 +478,10 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   };
   chk(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice), "desc upload");
   chk(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice), "begins upload");
-  // the cell-range table is never cleared again: an entry is valid only when
-  // the key stored at its start slot is the entry's own key
-  chk(cudaMemset(s->ranges, 0xff, sizeof(uint2) * std::max<uint64_t>(base, 1)), "range table init");
-  chk(cudaMemset(s->arena.base, 0, (char*)s->ranges - s->arena.base), "state init");
+  // everything starts at zero: the step epoch (flags[2]) is bumped to 1 by the
+  // first sort, so no range entry is valid before its cell is written; the
+  // table is never cleared again
+  chk(cudaMemset(s->arena.base, 0, s->arena.size), "state init");
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;
@@ -489,7 +546,7 @@ sphg_status sphg_preloop(sphg_sim* s, void* stream) {
   if (!s || !s->uploaded) return fail(SPHG_INVALID_ARG, "upload a state before the pre-loop");
   // PreLoopComputation: FindNeighbors -> density -> pressure -> forces.  The
   // forces are consumed at once by the fused integration of the next state.
-  SPHG_TRY(run_steps(s, 1, (cudaStream_t)stream));
+  SPHG_TRY(run_steps(s, 1, (cudaStream_t)stream, true));
   s->preloop_done = true;
   return SPHG_OK;
 }
@@ -591,8 +648,8 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
       SPHG_CUDA(cudaMemcpyAsync(v.data(), pos ? s->posB : s->velB, n * sizeof(float2),
                                 cudaMemcpyDeviceToHost, st));
       if (pos && s->opt.precision == SPHG_PRECISION_SPLIT) {
-        k.resize(n);
-        SPHG_CUDA(cudaMemcpyAsync(k.data(), s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        k.resize(n);  // the integrated offsets are relative to their new cells
+        SPHG_CUDA(cudaMemcpyAsync(k.data(), s->keyB, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
       }
       SPHG_CUDA(cudaStreamSynchronize(st));
       double* o = (double*)host;
@@ -638,16 +695,18 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
   sphg_status res = SPHG_OK;
   auto run = [&]() -> sphg_status {
     SPHG_CUDA(cudaEventRecord(ev[0], st));
-    SPHG_CUDA(sphg::launch_keys(a, prec, st));
     SPHG_CUDA(cudaEventRecord(ev[1], st));
     SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                     s->scratch, s->n, s->key_bits, st));
+                                     s->scratch, s->n, s->key_bits, st, s->flags + 2));
     SPHG_CUDA(cudaEventRecord(ev[2], st));
+    if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
     SPHG_CUDA(sphg::launch_reorder(a, st));
     SPHG_CUDA(cudaEventRecord(ev[3], st));
-    SPHG_CUDA(sphg::launch_density(a, prec, st));
+    if (s->tile_bits) SPHG_CUDA(sphg::launch_tiled(a, prec, false, st));
+    else SPHG_CUDA(sphg::launch_density(a, prec, st));
     SPHG_CUDA(cudaEventRecord(ev[4], st));
-    SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
+    if (s->tile_bits) SPHG_CUDA(sphg::launch_tiled(a, prec, true, st));
+    else SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
     SPHG_CUDA(cudaEventRecord(ev[5], st));
     SPHG_CUDA(cudaEventSynchronize(ev[5]));
     for (int i = 0; i < 5; ++i) SPHG_CUDA(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
@@ -661,7 +720,7 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
 int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
-  return 4 + 3 * passes;
+  return 3 + 3 * passes + (s->tile_bits ? 1 : 0);  // + the tile-counter reset
 }
 
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

@@ -43,6 +43,7 @@ struct __align__(16) InstDesc {
   float eps_h2;           // 0.01 h^2
   double lo_xd, lo_yd, cs_xd, cs_yd, Lx_d, Ly_d, h2_d;
   double mass_d, hi_xd, hi_yd;
+  double half_Lx_d, half_Ly_d;  // periodic minimum image
 };
 
 // ---------------------------------------------------------------- Morton codes
@@ -85,6 +86,10 @@ __device__ __forceinline__ void decode_code(const InstDesc& d, uint32_t code, in
 // (GenericNeighborSearch.h:216-222), from an FP32 position: the FP32 quotient
 // decides unless it lies within a few ulp of a cell edge, where the FP64
 // expression decides.  Clamped to [0, cmax] (the reference clamps above only).
+static __device__ __noinline__ int cell_coord_d(float x, double lo_d, double cs_d) {
+  return (int)floor(__ddiv_rn(__dsub_rn((double)x, lo_d), cs_d));
+}
+
 __device__ __forceinline__ int cell_coord(float x, float lo, float inv_cs, double lo_d,
                                           double cs_d, int cmax) {
   float q = (x - lo) * inv_cs;
@@ -97,14 +102,14 @@ __device__ __forceinline__ int cell_coord(float x, float lo, float inv_cs, doubl
   if (fr > tol && fr < 1.0f - tol) {
     c = (int)fq;
   } else {
-    c = (int)floor(__ddiv_rn(__dsub_rn((double)x, lo_d), cs_d));
+    c = cell_coord_d(x, lo_d, cs_d);  // out of line: keeps FP64 off the common path
   }
   return c < 0 ? 0 : (c > cmax ? cmax : c);
 }
 
 // FP64 distance test of the reference: r2 = dx*dx + dy*dy (no contraction),
 // inside when !(r2 > h2).
-static __device__ __noinline__ bool exact_inside_d(double dx, double dy, double h2_d) {
+static __device__ __forceinline__ bool exact_inside_d(double dx, double dy, double h2_d) {
   double r2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
   return !(r2 > h2_d);
 }

@@ -31,8 +31,8 @@ __global__ void __launch_bounds__(kListThreads) lists_count(StepArgs a, int32_t*
   if (i >= a.n) return;
   const InstDesc d = inst_of<BATCHED>(a, i);
   int cx, cy, c = 0;
-  for_each_neighbor<PREC>(a, d, a.keyA[i], a.posA[i], cx, cy,
-                          [&](uint32_t, float, float, float) { ++c; });
+  for_each_neighbor<PREC, true>(a, d, a.keyA[i], a.posA[i], cx, cy,
+                                [&](uint32_t, float, float, float, uint32_t) { ++c; });
   counts[i] = c;
 }
 
@@ -44,8 +44,8 @@ __global__ void __launch_bounds__(kListThreads) lists_fill(StepArgs a, const int
   const InstDesc d = inst_of<BATCHED>(a, i);
   int64_t o = offs[i];
   int cx, cy;
-  for_each_neighbor<PREC>(a, d, a.keyA[i], a.posA[i], cx, cy,
-                          [&](uint32_t j, float, float, float) { idx[o++] = (int32_t)j; });
+  for_each_neighbor<PREC, true>(a, d, a.keyA[i], a.posA[i], cx, cy,
+                                [&](uint32_t j, float, float, float, uint32_t) { idx[o++] = (int32_t)j; });
 }
 
 // Exclusive scan of int32 counts into int64 offsets (offs[n] = total).

@@ -27,8 +27,9 @@ constexpr int kWarps = kSortThreads / 32;
 __global__ void __launch_bounds__(kSortThreads) sort_hist(const uint32_t* __restrict__ keys,
                                                           int64_t n, int shift,
                                                           uint32_t* __restrict__ tile_hist,
-                                                          int ntiles) {
+                                                          int ntiles, uint32_t* epoch) {
   __shared__ uint32_t h[kRadix];
+  if (epoch && blockIdx.x == 0 && threadIdx.x == 0) *epoch += 1u;
   h[threadIdx.x] = 0;
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * kTile;
@@ -156,7 +157,7 @@ size_t sort_scratch_words(int64_t n) {
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, uint32_t* epoch) {
   if (n <= 0) return cudaSuccess;
   const int passes = bits <= 0 ? 1 : (bits + 7) / 8;
   const int ntiles = sort_num_tiles(n);
@@ -170,7 +171,8 @@ cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
     uint32_t* ko = to_out ? keys_out : keys_tmp;
     uint32_t* vo = to_out ? vals_out : vals_tmp;
     const int shift = 8 * p;
-    sort_hist<<<ntiles, kSortThreads, 0, stream>>>(kin, n, shift, tile_hist, ntiles);
+    sort_hist<<<ntiles, kSortThreads, 0, stream>>>(kin, n, shift, tile_hist, ntiles,
+                                                   p == 0 ? epoch : nullptr);
     sort_dscan<<<kRadix, 1024, 0, stream>>>(tile_hist, ntiles, digit_total);
     sort_scatter<<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, shift, tile_hist,
                                                       digit_total, ntiles);

@@ -12,10 +12,11 @@ size_t sort_scratch_words(int64_t n);
 // Stable sort of (keys_in, vals_in) on the low `bits` bits; vals_in == nullptr
 // means the identity 0..n-1.  keys_tmp/vals_tmp are ping-pong buffers of n
 // entries (unused for bits <= 8).  The result lands in keys_out/vals_out.
-// No buffer may alias another.
+// No buffer may alias another.  When epoch is not null the first pass
+// increments *epoch once (the step epoch of the cell-range table).
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
-                             cudaStream_t stream);
+                             cudaStream_t stream, uint32_t* epoch = nullptr);
 
 }  // namespace sphg

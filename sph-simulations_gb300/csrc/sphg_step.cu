@@ -28,16 +28,6 @@ namespace sphg {
 
 constexpr int kThreads = 256;
 
-// floor(o / cs) for a split-precision offset, FP64 near integer boundaries.
-__device__ __forceinline__ int offset_cells(float o, float inv_cs, double cs_d) {
-  float q = o * inv_cs;
-  float fq = floorf(q);
-  float fr = q - fq;
-  if (fr > 1.0e-6f && fr < 1.0f - 1.0e-6f && fabsf(q) < 1.0e6f) return (int)fq;
-  if (!(fabsf(q) < 1.0e6f)) return 0;  // NaN / runaway: leave the cell, the state is flagged elsewhere
-  return (int)floor(__ddiv_rn((double)o, cs_d));
-}
-
 // ---------------------------------------------------------------- keys
 template <int PREC, bool BATCHED>
 __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
@@ -86,8 +76,23 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
   a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
   if (a.track_ids) a.idsA[i] = a.idsB[src];
   uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
-  if (i == 0 || a.keyA[i - 1] != k) r[2 * (size_t)k] = (uint32_t)i;
-  if (i == a.n - 1 || a.keyA[i + 1] != k) r[2 * (size_t)k + 1] = (uint32_t)(i + 1);
+  const uint32_t kprev = i > 0 ? a.keyA[i - 1] : kNoIndex;
+  const uint32_t knext = i + 1 < a.n ? a.keyA[i + 1] : kNoIndex;
+  if (k != kprev) {
+    r[4 * (size_t)k] = (uint32_t)i;
+    r[4 * (size_t)k + 2] = *a.epoch;
+  }
+  if (k != knext) r[4 * (size_t)k + 1] = (uint32_t)(i + 1);
+  if (a.tile_bits) {
+    const int sh = 2 * a.tile_bits;
+    const uint32_t t = k >> sh;
+    uint32_t* tr = reinterpret_cast<uint32_t*>(a.tile_ranges);
+    if (kprev == kNoIndex || (kprev >> sh) != t) {
+      tr[2 * (size_t)t] = (uint32_t)i;
+      a.tile_list[atomicAdd(a.tile_count, 1u)] = t;
+    }
+    if (knext == kNoIndex || (knext >> sh) != t) tr[2 * (size_t)t + 1] = (uint32_t)(i + 1);
+  }
 }
 
 // ---------------------------------------------------------------- density + pressure
@@ -101,10 +106,19 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   typename std::conditional<PREC == 1, CSum, PSum>::type S;
   int cx, cy;
   const float inv_h2 = d.inv_h2;
-  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t, float, float, float r2) {
+  uint32_t* __restrict__ nbr = a.nbr;
+  const uint32_t slots = (uint32_t)a.nbr_slots;
+  const size_t n = (size_t)a.n;
+  uint32_t cnt = 0;
+  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
     float t = fmaf(-r2, inv_h2, 1.0f);
     S.add(t * t * t);
+    if (nbr && j != (uint32_t)i) {  // record the pair for the force pass
+      if (cnt < slots) nbr[cnt * n + i] = (j << 5) | tag;
+      ++cnt;
+    }
   });
+  if (nbr) a.ncount[i] = cnt;
   float rho, drho;
   if constexpr (PREC == 1) {
     rho = d.wd * S.value();
@@ -120,8 +134,17 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- forces (+ integration)
+// Accepted neighbours of a thread are first collected in shared memory
+// (dx, dy, j) by the cheap candidate scan, then the pair forces run over that
+// list: the warp executes the heavy per-pair math about max-over-lanes(count)
+// times instead of once per candidate iteration.  A thread with more than
+// kForceBuf neighbours handles the extra ones inline during the scan.
+constexpr int kForceBuf = 12;
+
 template <int PREC, bool BATCHED, int MODE>
 __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
+  __shared__ float2 bd[kForceBuf][kThreads];
+  __shared__ uint32_t bj[kForceBuf][kThreads];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const InstDesc d = inst_of<BATCHED>(a, i);
@@ -133,9 +156,8 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
   const float alpha_c0 = d.alpha_c0;
   const float4* __restrict__ velp = a.velpA;
-  int cx, cy;
-  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float dx, float dy, float r2) {
-    if (j == (uint32_t)i) return;
+  auto pair = [&](uint32_t j, float dx, float dy) {
+    const float r2 = fmaf(dx, dx, dy * dy);
     const float4 vj = __ldg(velp + j);
     const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
     const float r = r2 * rinv;
@@ -159,7 +181,47 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
         fay.add(s * dy);
       }
     }
-  });
+  };
+  int cx, cy;
+  const uint32_t cnt = a.nbr ? a.ncount[i] : 0xffffffffu;
+  if (cnt <= (uint32_t)a.nbr_slots) {
+    // the density pass recorded this particle's neighbours (stencil order)
+    decode_code(d, key - d.cell_base, cx, cy);
+    const size_t n = (size_t)a.n;
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const uint32_t e = __ldg(a.nbr + q * n + i);
+      const uint32_t j = e >> 5, k = e & 15u;
+      const float2 pj = __ldg(a.posA + j);
+      float dx, dy;
+      if (PREC == 0 && (e & 16u)) {
+        wrapped_pair(d, pi, pj, dx, dy);
+      } else {
+        const int c1 = (int)(k / 3) - 1, c2 = (int)(k % 3) - 1;
+        const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
+        const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
+        dx = (pi.x - pj.x) - shx;
+        dy = (pi.y - pj.y) - shy;
+      }
+      pair(j, dx, dy);
+    }
+  } else {
+    int nb = 0;
+    const int t = threadIdx.x;
+    for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float dx, float dy, float, uint32_t) {
+      if (j == (uint32_t)i) return;
+      if (nb < kForceBuf) {
+        bd[nb][t] = make_float2(dx, dy);
+        bj[nb][t] = j;
+        ++nb;
+      } else {
+        pair(j, dx, dy);
+      }
+    });
+    for (int q = 0; q < nb; ++q) {
+      const float2 dd = bd[q][t];
+      pair(bj[q][t], dd.x, dd.y);
+    }
+  }
   float ax = d.gx + fpx.value();
   float ay = d.gy + fpy.value();
   ax += fvx.value();
@@ -172,39 +234,7 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
     a.acc[i] = make_float2(ax, ay);
     return;
   }
-  // symplectic Euler (UpdateVelocities then UpdatePositions) + boundary
-  const float dt = d.dt;
-  float vx = fmaf(dt, ax, vi.x);
-  float vy = fmaf(dt, ay, vi.y);
-  float x = fmaf(dt, vx, pi.x);
-  float y = fmaf(dt, vy, pi.y);
-  if (d.periodic) {
-    if (PREC == 0) {
-      if (x >= d.hi_x) x -= d.Lx;
-      if (x < d.lo_x) x += d.Lx;
-      if (y >= d.hi_y) y -= d.Ly;
-      if (y < d.lo_y) y += d.Ly;
-    }
-    // split precision: the cell index wraps in step_keys, the offset is unchanged
-  } else {
-    float whx, wlx, why, wly;  // walls in the particle's frame
-    if (PREC == 0) {
-      whx = d.hi_x; wlx = d.lo_x; why = d.hi_y; wly = d.lo_y;
-    } else {
-      whx = d.Lx - (float)cx * d.cs_x;
-      wlx = -(float)cx * d.cs_x;
-      why = d.Ly - (float)cy * d.cs_y;
-      wly = -(float)cy * d.cs_y;
-    }
-    // Integrator::ApplyBoundaryConditions (Integrator.cpp:30-46): per axis high then low
-    if (x > whx) { x = whx; vx = -vx; }
-    if (x < wlx) { x = wlx; vx = -vx; }
-    if (y > why) { y = why; vy = -vy; }
-    if (y < wly) { y = wly; vy = -vy; }
-  }
-  a.posB[i] = make_float2(x, y);
-  a.velB[i] = make_float2(vx, vy);
-  if (a.track_ids) a.idsB[i] = a.idsA[i];
+  integrate_and_key<PREC>(a, d, i, cx, cy, pi, vi, ax, ay);
 }
 
 // ---------------------------------------------------------------- diagnostics

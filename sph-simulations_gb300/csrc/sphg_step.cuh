@@ -21,7 +21,8 @@ struct StepArgs {
   float4* velpA;               // (vx, vy, p/rho^2, 1/rho)
   float* rho;
   uint32_t* keyA;              // sorted global keys
-  uint2* ranges;               // [total keys]
+  uint4* ranges;               // [total keys] {start, end, epoch, 0}
+  const uint32_t* epoch;       // current step's epoch (bumped by the sort)
   int32_t* idsA;
   // integrated ("next") state in the current slot order
   float2* posB;
@@ -30,7 +31,17 @@ struct StepArgs {
   int32_t* idsB;
   uint32_t* perm;              // sort output: previous slot of each new slot
   float2* acc;                 // forces (only written on request)
-  uint32_t* flags;             // [0] non-finite count (diagnostics)
+  uint32_t* nbr;               // [nbr_slots][n] neighbours found by the density pass: j << 5 | tag
+  uint32_t* ncount;            // [n] neighbours of each particle (> nbr_slots: list overflowed)
+  int nbr_slots;
+  uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
+  // cell tiles (Morton order only; tile_bits == 0 disables them)
+  int tile_bits;               // tiles of 2^tile_bits x 2^tile_bits cells
+  int tile_cap;                // shared-memory staging capacity (particles)
+  int tile_grid;               // CTAs of the tile kernels
+  uint2* tile_ranges;          // [total keys >> 2*tile_bits] particle run of each tile
+  uint32_t* tile_list;         // ids of this step's non-empty tiles
+  uint32_t* tile_count;        // device counter (= flags + 1)
 };
 
 enum ForceMode { kForceIntegrate = 0, kForceOnly = 1 };
@@ -47,6 +58,9 @@ int diag_chunks(int64_t max_inst_n);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
                cudaStream_t st, std::string* err);
+// Cell-tile density (force == false) or force + integration + next keys (force == true).
+cudaError_t launch_tiled(const StepArgs& a, int precision, bool force, cudaStream_t s);
+size_t tile_smem_bytes(int tb, int cap, bool force);
 // Records the message returned by sphg_last_error_string() (sphg_api.cu).
 void set_last_error(const std::string& msg);
 cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const float* y, int64_t n,

@@ -39,7 +39,7 @@ class Params(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32)]
 
 
 _lib = None
@@ -107,12 +107,13 @@ def params(**kw):
     return p
 
 
-def options(precision=PLAIN, track_ids=1, use_graph=1):
+def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0):
     o = Options()
     lib().sphg_default_options(ctypes.byref(o))
     o.precision = precision
     o.track_ids = track_ids
     o.use_graph = use_graph
+    o.tile_bits = tile_bits
     return o
 
 

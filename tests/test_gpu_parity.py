@@ -215,9 +215,9 @@ def test_step_chain_teacher_forced(order):
             assert np.all(np.abs(got - ref) <= 4 * np.spacing(np.abs(ref).astype(np.float32)) + 1e-12)
         for got, ref in ((nvx, ovx), (nvy, ovy)):
             assert np.all(np.abs(got - ref) <= 4 * np.spacing(np.abs(ref).astype(np.float32)) + 1e-9)
-        sim.step(1)
         # keys of the integrated state, computed from the same FP32 positions
         assert (sim.debug(S.DBG_UNSORTED_KEYS) == O.cell_ids(p, nx_, ny_)).all()
+        sim.step(1)
         perm = sim.debug(S.DBG_PERM)
         assert (perm == O.sort_perm(O.cell_ids(p, nx_, ny_))).all()
         b = sim.download(forces=False)
@@ -369,3 +369,55 @@ def test_split_and_plain_agree_over_many_steps():
     assert np.max(np.abs(out[0][0] - out[1][0])) < 1e-5
     assert np.max(np.abs(out[0][1] - out[1][1])) < 1e-5
     assert out[1][2][2] == len(x) and out[1][2][5] == 0
+
+
+# ---------------------------------------------------------------- cell-tile kernels
+@pytest.mark.parametrize("prec", ["plain", "split"])
+@pytest.mark.parametrize("tb", [3, 4, 5])
+def test_tiled_kernels_match_oracle_and_untiled(prec, tb):
+    S = _sphg()
+    dx = 0.005
+    x, y, vx, vy = jittered(80, 160, dx, seed=9, vel=0.3)
+    kw = dict(order="morton", h=1.3 * dx, dt=1e-5, k=30.0, rho0=1000.0, gy=-9.81,
+              mass=1.3e-4, alpha=0.1, lo=(0, 0), hi=(1, 1))
+    p = O.params(**kw)
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    res = {}
+    for t in (tb, -1):
+        sim = S.Sim(S.params(**kw), len(x), S.options(precision=P, tile_bits=t))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        sim.step(3)
+        a = sim.download()
+        nxt = sim.debug(S.DBG_POS_NEXT)
+        res[t] = (a, nxt, sim.debug(S.DBG_UNSORTED_KEYS))
+        sk, s, e, rho, fx, fy = oracle_state(p, a)
+        assert rel_rho(a["rho"], rho) <= RHO_TOL
+        assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+        sim.close()
+    a, b = res[tb][0], res[-1][0]
+    assert (a["ids"] == b["ids"]).all()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_allclose(a[k], b[k], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(a["rho"], b["rho"], rtol=1e-6)
+
+
+def test_tile_overflow_falls_back_to_global_walk():
+    """A clump far denser than the shared-memory staging capacity."""
+    S = _sphg()
+    rng = np.random.default_rng(12)
+    h = 0.01
+    n = 3000
+    x = (0.5 + rng.uniform(-1.5 * h, 1.5 * h, n)).astype(np.float32).astype(np.float64)
+    y = (0.5 + rng.uniform(-1.5 * h, 1.5 * h, n)).astype(np.float32).astype(np.float64)
+    z = np.zeros(n)
+    kw = dict(order="morton", h=h, dt=1e-6, lo=(0, 0), hi=(1, 1))
+    p = O.params(**kw)
+    sim = S.Sim(S.params(**kw), n, S.options(tile_bits=3))
+    sim.upload(x, y, z, z)
+    sim.preloop()
+    a = sim.download()
+    sk, s, e, rho, fx, fy = oracle_state(p, a)
+    assert rel_rho(a["rho"], rho) <= RHO_TOL
+    assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+    sim.close()
