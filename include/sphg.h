@@ -150,13 +150,14 @@ int32_t sphg_launches_per_step(const sphg_sim* s);
  * keys_out/vals_out must not alias the inputs.  Scratch is allocated by this call. */
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                             uint32_t* vals_out, int64_t n, int32_t bits, void* stream);
-/* Largest n sphg_sort_pairs_noalloc accepts. */
+/* Largest n sphg_sort_pairs_noalloc accepts, and the size of its fixed scratch. */
 #define SPHG_SORT_NOALLOC_MAX_PAIRS 262144
+#define SPHG_SORT_NOALLOC_SCRATCH_BYTES 2626560
 /* sphg_sort_pairs for callers that cannot allocate device memory when they
  * sort (allocation-free graph capture, fixed-budget allocators, hosts that
  * forbid cudaMalloc).  No counterpart in the reference.  Same arguments and
  * result as sphg_sort_pairs, but its scratch is a fixed device array inside
- * the library (2,229,248 bytes, held on every GPU that loads the library until
+ * the library (SPHG_SORT_NOALLOC_SCRATCH_BYTES = 2,626,560 bytes, held on every GPU that loads the library until
  * the process exits), so n must be <= SPHG_SORT_NOALLOC_MAX_PAIRS
  * (SPHG_CAPACITY otherwise).  It calls no cudaMalloc/cudaFree.  The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress);

@@ -258,6 +258,8 @@ struct sphg_sim {
     a.tile_list = tile_list;
     a.tile_count = flags + 1;
     a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
+    a.ghist = nullptr;  // the sort computes its digit histograms itself
+    a.key_passes = (key_bits + 7) / 8;
     a.ncount = ncount;
     a.nbr_slots = nbr_slots;
     return a;
@@ -272,8 +274,10 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
   if (first) SPHG_CUDA(sphg::launch_keys(a, prec, st));
+  // the key writers (key pass / force pass) accumulated the digit histograms
   SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                   s->scratch, s->n, s->key_bits, st, s->flags + 2));
+                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist));
+  if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
   if (s->tile_bits) {
@@ -535,6 +539,8 @@ sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const dou
       for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
       SPHG_CUDA(cudaMemcpyAsync(s->idsB, ids.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     }
+    // digit histograms of the next sort restart with the uploaded state
+    SPHG_CUDA(cudaMemsetAsync(s->scratch, 0, sizeof(uint32_t) * 4 * 256, st));
     SPHG_CUDA(cudaStreamSynchronize(st));
   }
   s->uploaded = true;
@@ -697,7 +703,8 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
     SPHG_CUDA(cudaEventRecord(ev[0], st));
     SPHG_CUDA(cudaEventRecord(ev[1], st));
     SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                     s->scratch, s->n, s->key_bits, st, s->flags + 2));
+                                     s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist));
+    if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
     SPHG_CUDA(cudaEventRecord(ev[2], st));
     if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
     SPHG_CUDA(sphg::launch_reorder(a, st));
@@ -720,7 +727,8 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
 int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
-  return 3 + 3 * passes + (s->tile_bits ? 1 : 0);  // + the tile-counter reset
+  // radix passes + reorder + density + force (+ the sort's histogram kernel with tiles)
+  return passes + 3 + (s->tile_bits ? 1 : 0);
 }
 
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

@@ -233,7 +233,7 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
 // the next sort (SetParticleCellIds).  Split precision keeps the position as
 // (cell, offset) and renormalises the offset into the new cell.
 template <int PREC>
-__device__ __forceinline__ void integrate_and_key(const StepArgs& a, const InstDesc& d, int64_t i,
+__device__ __forceinline__ uint32_t integrate_and_key(const StepArgs& a, const InstDesc& d, int64_t i,
                                                   int cx, int cy, float2 pi, float4 vi, float ax,
                                                   float ay) {
   const float dt = d.dt;
@@ -286,10 +286,29 @@ __device__ __forceinline__ void integrate_and_key(const StepArgs& a, const InstD
       y -= (float)(ny_ - cy) * d.cs_y;
     }
   }
+  const uint32_t key = d.cell_base + local_code(d, nx_, ny_);
   a.posB[i] = make_float2(x, y);
   a.velB[i] = make_float2(vx, vy);
-  a.keyB[i] = d.cell_base + local_code(d, nx_, ny_);
+  a.keyB[i] = key;
   if (a.track_ids) a.idsB[i] = a.idsA[i];
+  return key;
+}
+
+// Adds one key per thread (valid == false: none) to the radix digit histograms
+// of the next sort: block-level counts in shared memory, then one global atomic
+// per (pass, digit).  Call with the whole block.
+__device__ __forceinline__ void histogram_keys(const StepArgs& a, uint32_t (*hs)[256], bool valid,
+                                               uint32_t key) {
+  const int lane = threadIdx.x & 31;
+  for (int p = 0; p < a.key_passes; ++p) {
+    const uint32_t dg = valid ? (key >> (8 * p)) & 255u : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, dg);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&hs[p][dg], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  for (int p = 0; p < a.key_passes; ++p)
+    for (int t = threadIdx.x; t < 256; t += blockDim.x)
+      if (hs[p][t]) atomicAdd(&a.ghist[p * 256 + t], hs[p][t]);
 }
 
 }  // namespace sphg

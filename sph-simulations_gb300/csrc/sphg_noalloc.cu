@@ -26,11 +26,11 @@
 namespace {
 
 constexpr int64_t kNoAllocMaxPairs = SPHG_SORT_NOALLOC_MAX_PAIRS;
-constexpr int64_t kTileKeys = 2048;  // keys per sort tile (sphg_sort.cu)
-constexpr size_t kHistWords = 256 * ((kNoAllocMaxPairs + kTileKeys - 1) / kTileKeys) + 256;
+constexpr size_t kHistWords = sphg::sort_scratch_words_c(kNoAllocMaxPairs);
 constexpr size_t kScratchWords = kHistWords + 2 * (size_t)kNoAllocMaxPairs;
+static_assert(kScratchWords * 4 == SPHG_SORT_NOALLOC_SCRATCH_BYTES, "documented scratch size");
 
-// [tile histograms + digit totals | ping-pong keys | ping-pong values]
+// [histograms, tile counters, error word, look-back words | ping-pong keys | ping-pong values]
 static __device__ __align__(256) uint32_t g_noalloc_sort_scratch[kScratchWords];
 
 constexpr int kMaxDevices = 64;
@@ -78,7 +78,8 @@ sphg_status sphg_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* val
   uint32_t* scratch = nullptr;
   sphg_status st = scratch_for_current_device(&scratch);
   if (st != SPHG_OK) return st;
-  // The histogram words are fully rewritten by every pass; nothing needs clearing.
+  // The sort clears its histograms, tile counters and look-back words itself
+  // (stream-ordered memsets, no allocation) before each use.
   uint32_t* keys_tmp = scratch + kHistWords;
   uint32_t* vals_tmp = keys_tmp + kNoAllocMaxPairs;
   cudaError_t e = sphg::radix_sort_pairs(keys_in, vals_in, keys_out, vals_out, keys_tmp, vals_tmp,

@@ -4,13 +4,16 @@
 // (core/acceleration/cuFindNeighbors.cu:82-100), sorting the slot index
 // instead of six payload arrays; the payload is gathered once afterwards.
 //
-// One pass per 8-bit digit, three kernels per pass:
-//   sort_hist      per-tile digit histogram (warp-aggregated shared atomics)
-//   sort_dscan     per-digit exclusive scan over tiles (one CTA per digit)
-//   sort_scatter   stable in-tile ranking (__match_any_sync + popc across the
-//                  tile's rounds and warps) and scatter to the global offsets
-// Tiles are 2048 keys (256 threads x 8 items, striped so that a round of 256
-// consecutive keys is ranked before the next round -> stability).
+// One-sweep structure, 8-bit digits:
+//   sort_hist_all   one read of the keys -> digit histograms of every pass
+//   sort_pass       one kernel per pass: a CTA takes the next tile of 2048 keys
+//                   (tile ids handed out in start order by an atomic counter),
+//                   ranks them stably in registers (__match_any_sync + popc,
+//                   rounds of 256 consecutive keys), publishes its per-digit
+//                   counts, finds its global offsets by a decoupled look-back
+//                   over the preceding tiles' published counts, and scatters.
+// The look-back only waits on tiles that started earlier (so it cannot
+// deadlock); each wait is bounded and sets an error word if it gives up.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -23,85 +26,93 @@ constexpr int kSortItems = 8;
 constexpr int kTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 constexpr int kWarps = kSortThreads / 32;
+constexpr int kMaxPasses = 4;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPre = 2u << 30;
+constexpr uint32_t kValMask = kFlagAgg - 1u;
+constexpr int kSpinLimit = 1 << 22;
 
-__global__ void __launch_bounds__(kSortThreads) sort_hist(const uint32_t* __restrict__ keys,
-                                                          int64_t n, int shift,
-                                                          uint32_t* __restrict__ tile_hist,
-                                                          int ntiles, uint32_t* epoch) {
-  __shared__ uint32_t h[kRadix];
-  if (epoch && blockIdx.x == 0 && threadIdx.x == 0) *epoch += 1u;
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kTile;
-  const int lane = threadIdx.x & 31;
-  for (int k = 0; k < kSortItems; ++k) {
-    int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
-    bool valid = i < n;
-    uint32_t d = valid ? (__ldg(keys + i) >> shift) & (kRadix - 1) : kRadix;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
-  }
-  __syncthreads();
-  tile_hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+static inline int passes_for(int bits) { return bits <= 0 ? 1 : (bits + 7) / 8; }
+
+int sort_num_tiles(int64_t n) { return (int)((n + kTile - 1) / kTile); }
+
+// scratch: [passes x 256 histogram][passes tile counters][error word][pad to 256]
+//          [passes x ntiles x 256 look-back words]
+static inline size_t head_words() { return (size_t)kMaxPasses * kRadix + 256; }
+
+size_t sort_scratch_words(int64_t n) {
+  return head_words() + (size_t)kMaxPasses * kRadix * (size_t)sort_num_tiles(n);
 }
+static_assert(kMaxPasses * kRadix + 256 == 1280 && kTile == 2048, "sort_scratch_words_c layout");
 
-// One CTA per digit: exclusive scan of tile_hist[d][0..ntiles), total -> digit_total[d].
-__global__ void __launch_bounds__(1024) sort_dscan(uint32_t* __restrict__ tile_hist, int ntiles,
-                                                   uint32_t* __restrict__ digit_total) {
-  __shared__ uint32_t warp_sums[32];
-  __shared__ uint32_t carry_s;
-  uint32_t* row = tile_hist + (int64_t)blockIdx.x * ntiles;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) carry_s = 0;
+// Digit histograms of every pass in one read of the keys.  Each thread counts
+// a run of 16 consecutive keys; nearly sorted input has long runs of equal
+// digits, so one shared atomic per run and pass replaces one per key.
+constexpr int kHistPerThread = 16;
+
+__global__ void __launch_bounds__(kSortThreads) sort_hist_all(const uint32_t* __restrict__ keys,
+                                                              int64_t n, int passes,
+                                                              uint32_t* __restrict__ ghist) {
+  __shared__ uint32_t h[kMaxPasses][kRadix];
+  for (int p = 0; p < kMaxPasses; ++p) h[p][threadIdx.x] = 0;
   __syncthreads();
-  for (int base = 0; base < ntiles; base += 1024) {
-    int t = base + threadIdx.x;
-    uint32_t v = t < ntiles ? row[t] : 0;
-    uint32_t x = v;
+  const int64_t chunk = (int64_t)kSortThreads * kHistPerThread;
+  for (int64_t b = (int64_t)blockIdx.x * chunk; b < n; b += (int64_t)gridDim.x * chunk) {
+    const int64_t s0 = b + (int64_t)threadIdx.x * kHistPerThread;
+    uint32_t k[kHistPerThread];
+    if (s0 + kHistPerThread <= n && ((s0 & 3) == 0)) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t s = warp_sums[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += y;
+      for (int q = 0; q < kHistPerThread; q += 4) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(keys + s0 + q));
+        k[q] = v.x; k[q + 1] = v.y; k[q + 2] = v.z; k[q + 3] = v.w;
       }
-      warp_sums[lane] = s;  // inclusive over warps
+    } else {
+#pragma unroll
+      for (int q = 0; q < kHistPerThread; ++q) k[q] = s0 + q < n ? __ldg(keys + s0 + q) : 0u;
     }
-    __syncthreads();
-    uint32_t carry = carry_s;
-    uint32_t excl = carry + (warp ? warp_sums[warp - 1] : 0) + x - v;
-    if (t < ntiles) row[t] = excl;
-    __syncthreads();
-    if (threadIdx.x == 0) carry_s = carry + warp_sums[31];
-    __syncthreads();
+    const int m = (int)(s0 >= n ? 0 : (n - s0 < kHistPerThread ? n - s0 : kHistPerThread));
+    for (int p = 0; p < passes; ++p) {
+      uint32_t run_d = 0, run_c = 0;
+#pragma unroll
+      for (int q = 0; q < kHistPerThread; ++q) {
+        if (q >= m) break;
+        const uint32_t d = (k[q] >> (8 * p)) & (kRadix - 1);
+        if (run_c && d != run_d) {
+          atomicAdd(&h[p][run_d], run_c);
+          run_c = 0;
+        }
+        run_d = d;
+        ++run_c;
+      }
+      if (run_c) atomicAdd(&h[p][run_d], run_c);
+    }
   }
-  if (threadIdx.x == 0) digit_total[blockIdx.x] = carry_s;
+  __syncthreads();
+  for (int p = 0; p < passes; ++p)
+    if (h[p][threadIdx.x]) atomicAdd(&ghist[p * kRadix + threadIdx.x], h[p][threadIdx.x]);
 }
 
-__global__ void __launch_bounds__(kSortThreads) sort_scatter(
+template <int ITEMS>
+__global__ void __launch_bounds__(kSortThreads) sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int shift,
-    const uint32_t* __restrict__ tile_hist, const uint32_t* __restrict__ digit_total,
-    int ntiles) {
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int pass,
+    const uint32_t* __restrict__ ghist, uint32_t* tile_counter, uint32_t* lookback,
+    uint32_t* err, uint32_t* epoch) {
+  __shared__ uint32_t s_tile;
   __shared__ uint32_t base_s[kRadix];
   __shared__ uint32_t running[kRadix];
   __shared__ uint32_t warp_cnt[kWarps][kRadix];
   __shared__ uint32_t wsum[kWarps];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int shift = 8 * pass;
 
-  // global start of digit tid = exclusive scan of digit_total + this tile's offset
-  uint32_t tot = digit_total[tid];
+  if (tid == 0) s_tile = atomicAdd(tile_counter + pass, 1u);
+  // start of digit tid in the output: exclusive scan of this pass's histogram
+  const uint32_t tot = ghist[pass * kRadix + tid];
   uint32_t x = tot;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
   if (lane == 31) wsum[warp] = x;
@@ -109,32 +120,38 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter(
 #pragma unroll
   for (int w = 0; w < kWarps; ++w) warp_cnt[w][tid] = 0;
   __syncthreads();
-  uint32_t wpre = 0;
-  for (int w = 0; w < warp; ++w) wpre += wsum[w];
-  base_s[tid] = wpre + x - tot + tile_hist[(int64_t)tid * ntiles + blockIdx.x];
-  __syncthreads();
+  uint32_t dstart = x - tot;
+  for (int w = 0; w < warp; ++w) dstart += wsum[w];
+  const uint32_t tile = s_tile;
+  const int64_t base = (int64_t)tile * (kSortThreads * ITEMS);
+  if (epoch && tile == 0 && tid == 0) *epoch += 1u;  // nobody reads the epoch during the sort
 
-  const int64_t base = (int64_t)blockIdx.x * kTile;
-  const unsigned lt_mask = (1u << lane) - 1u;
-  for (int k = 0; k < kSortItems; ++k) {
-    int64_t i = base + (int64_t)k * kSortThreads + tid;
-    bool valid = i < n;
-    uint32_t key = 0, val = 0, d = kRadix;
-    if (valid) {
-      key = __ldg(keys_in + i);
-      val = vals_in ? __ldg(vals_in + i) : (uint32_t)i;
-      d = (key >> shift) & (kRadix - 1);
+  // load the tile (striped: round k holds keys base + k*256 + tid)
+  uint32_t key[ITEMS], val[ITEMS], rank[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int64_t i = base + (int64_t)k * kSortThreads + tid;
+    if (i < n) {
+      key[k] = __ldg(keys_in + i);
+      val[k] = vals_in ? __ldg(vals_in + i) : (uint32_t)i;
+    } else {
+      key[k] = 0;
+      val[k] = 0;
     }
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    uint32_t rank = __popc(peers & lt_mask);
+  }
+  // stable in-tile ranks
+  const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const bool valid = base + (int64_t)k * kSortThreads + tid < n;
+    const uint32_t d = valid ? (key[k] >> shift) & (kRadix - 1) : kRadix;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
     if (valid && lane == __ffs(peers) - 1) warp_cnt[warp][d] = __popc(peers);
     __syncthreads();
     if (valid) {
       uint32_t pre = 0;
       for (int w = 0; w < warp; ++w) pre += warp_cnt[w][d];
-      uint32_t pos = base_s[d] + running[d] + pre + rank;
-      keys_out[pos] = key;
-      vals_out[pos] = val;
+      rank[k] = running[d] + pre + __popc(peers & lt_mask);
     }
     __syncthreads();
     uint32_t s = 0;
@@ -146,40 +163,113 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter(
     running[tid] += s;
     __syncthreads();
   }
-}
 
-int sort_num_tiles(int64_t n) { return (int)((n + kTile - 1) / kTile); }
+  // publish this tile's count of digit tid, then look back for the exclusive prefix
+  const uint32_t cnt = running[tid];
+  uint32_t* my = lookback + (size_t)tile * kRadix + tid;
+  uint32_t excl = 0;
+  if (tile == 0) {
+    atomicExch(my, kFlagPre | cnt);
+  } else {
+    atomicExch(my, kFlagAgg | cnt);
+    // walk back eight predecessors per round trip: add their counts until one
+    // carries an inclusive prefix
+    int64_t t = (int64_t)tile - 1;
+    int spins = 0;
+    bool done = false;
+    while (!done && t >= 0) {
+      uint32_t w[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        w[q] = (t - q >= 0) ? *((const volatile uint32_t*)(lookback + (size_t)(t - q) * kRadix + tid))
+                            : kFlagPre;
+      int used = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (done || used < q) continue;  // stop at the first word not yet published
+        const uint32_t v = w[q];
+        if ((v & (kFlagAgg | kFlagPre)) == 0) continue;
+        excl += v & kValMask;
+        used = q + 1;
+        if (v & kFlagPre) done = true;
+      }
+      t -= used;
+      if (!done && used < 8 && t >= 0) {
+        if (++spins > kSpinLimit) {  // give up: flag the error, treat the rest as zero
+          atomicExch(err, 1u);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    atomicExch(my, kFlagPre | (excl + cnt));
+  }
+  base_s[tid] = dstart + excl;
+  __syncthreads();
 
-size_t sort_scratch_words(int64_t n) {
-  return (size_t)kRadix * (size_t)sort_num_tiles(n) + kRadix;
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int64_t i = base + (int64_t)k * kSortThreads + tid;
+    if (i < n) {
+      const uint32_t d = (key[k] >> shift) & (kRadix - 1);
+      const uint32_t pos = base_s[d] + rank[k];
+      keys_out[pos] = key[k];
+      vals_out[pos] = val[k];
+    }
+  }
 }
 
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
-                             cudaStream_t stream, uint32_t* epoch) {
+                             cudaStream_t stream, uint32_t* epoch, const uint32_t* hist) {
   if (n <= 0) return cudaSuccess;
-  const int passes = bits <= 0 ? 1 : (bits + 7) / 8;
-  const int ntiles = sort_num_tiles(n);
-  uint32_t* tile_hist = scratch;
-  uint32_t* digit_total = scratch + (size_t)kRadix * ntiles;
+  const int passes = passes_for(bits);
+  // big inputs: 4096-key tiles halve the look-back chain; small ones: 2048 for parallelism
+  const int items = n >= (1 << 18) ? 16 : 8;
+  const int ntiles = (int)((n + kSortThreads * items - 1) / (kSortThreads * items));
+  uint32_t* ghist = scratch;
+  uint32_t* tile_counter = scratch + kMaxPasses * kRadix;
+  uint32_t* err = tile_counter + kMaxPasses;
+  uint32_t* lookback = scratch + head_words();
+  // tile counters and look-back words start at zero every sort; so does the
+  // histogram unless the caller accumulated it already (the error word is left
+  // alone: it stays set until the caller clears it)
+  cudaError_t e;
+  if (hist) {
+    e = cudaMemsetAsync(tile_counter, 0, sizeof(uint32_t) * kMaxPasses, stream);
+  } else {
+    e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + kMaxPasses), stream);
+  }
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * (size_t)passes * kRadix * ntiles, stream);
+  if (e != cudaSuccess) return e;
+  if (!hist) {
+    const int64_t hchunks = (n + kSortThreads * kHistPerThread - 1) / (kSortThreads * kHistPerThread);
+    const int hist_blocks = (int)(hchunks < 608 ? hchunks : 608);
+    sort_hist_all<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, n, passes, ghist);
+    hist = ghist;
+  }
   const uint32_t* kin = keys_in;
   const uint32_t* vin = vals_in;
   for (int p = 0; p < passes; ++p) {
-    // the last pass lands in keys_out/vals_out
-    bool to_out = ((passes - 1 - p) % 2) == 0;
+    const bool to_out = ((passes - 1 - p) % 2) == 0;  // the last pass lands in keys_out
     uint32_t* ko = to_out ? keys_out : keys_tmp;
     uint32_t* vo = to_out ? vals_out : vals_tmp;
-    const int shift = 8 * p;
-    sort_hist<<<ntiles, kSortThreads, 0, stream>>>(kin, n, shift, tile_hist, ntiles,
-                                                   p == 0 ? epoch : nullptr);
-    sort_dscan<<<kRadix, 1024, 0, stream>>>(tile_hist, ntiles, digit_total);
-    sort_scatter<<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, shift, tile_hist,
-                                                      digit_total, ntiles);
+    if (items == 16)
+      sort_pass<16><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, p, hist, tile_counter,
+                                                         lookback + (size_t)p * kRadix * ntiles, err,
+                                                         p == 0 ? epoch : nullptr);
+    else
+      sort_pass<8><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, p, hist, tile_counter,
+                                                        lookback + (size_t)p * kRadix * ntiles, err,
+                                                        p == 0 ? epoch : nullptr);
     kin = ko;
     vin = vo;
   }
   return cudaGetLastError();
 }
+
+uint32_t* sort_error_word(uint32_t* scratch) { return scratch + kMaxPasses * kRadix + kMaxPasses; }
 
 }  // namespace sphg

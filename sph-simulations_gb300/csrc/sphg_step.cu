@@ -31,37 +31,45 @@ constexpr int kThreads = 256;
 // ---------------------------------------------------------------- keys
 template <int PREC, bool BATCHED>
 __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
+  __shared__ uint32_t hs[4][256];
+  for (int p = 0; p < 4; ++p) hs[p][threadIdx.x] = 0;
+  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const InstDesc d = inst_of<BATCHED>(a, i);
-  float2 p = a.posB[i];
-  const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
-  const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
-  int cx, cy;
-  if (PREC == 0) {
-    cx = cell_coord(p.x, d.lo_x, d.inv_cs_x, d.lo_xd, d.cs_xd, cmx);
-    cy = cell_coord(p.y, d.lo_y, d.inv_cs_y, d.lo_yd, d.cs_yd, cmy);
-  } else {
-    int ox, oy;
-    decode_code(d, a.keyA[i] - d.cell_base, ox, oy);
-    int kx = offset_cells(p.x, d.inv_cs_x, d.cs_xd);
-    int ky = offset_cells(p.y, d.inv_cs_y, d.cs_yd);
-    cx = ox + kx;
-    cy = oy + ky;
-    if (d.periodic) {
-      p.x -= (float)kx * d.cs_x;
-      p.y -= (float)ky * d.cs_y;
-      cx = ((cx % d.nxr) + d.nxr) % d.nxr;
-      cy = ((cy % d.nyr) + d.nyr) % d.nyr;
+  const bool valid = i < a.n;
+  uint32_t key = 0;
+  if (valid) {
+    const InstDesc d = inst_of<BATCHED>(a, i);
+    float2 p = a.posB[i];
+    const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
+    const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
+    int cx, cy;
+    if (PREC == 0) {
+      cx = cell_coord(p.x, d.lo_x, d.inv_cs_x, d.lo_xd, d.cs_xd, cmx);
+      cy = cell_coord(p.y, d.lo_y, d.inv_cs_y, d.lo_yd, d.cs_yd, cmy);
     } else {
-      cx = cx < 0 ? 0 : (cx > cmx ? cmx : cx);
-      cy = cy < 0 ? 0 : (cy > cmy ? cmy : cy);
-      p.x -= (float)(cx - ox) * d.cs_x;
-      p.y -= (float)(cy - oy) * d.cs_y;
+      int ox, oy;
+      decode_code(d, a.keyA[i] - d.cell_base, ox, oy);
+      int kx = offset_cells(p.x, d.inv_cs_x, d.cs_xd);
+      int ky = offset_cells(p.y, d.inv_cs_y, d.cs_yd);
+      cx = ox + kx;
+      cy = oy + ky;
+      if (d.periodic) {
+        p.x -= (float)kx * d.cs_x;
+        p.y -= (float)ky * d.cs_y;
+        cx = ((cx % d.nxr) + d.nxr) % d.nxr;
+        cy = ((cy % d.nyr) + d.nyr) % d.nyr;
+      } else {
+        cx = cx < 0 ? 0 : (cx > cmx ? cmx : cx);
+        cy = cy < 0 ? 0 : (cy > cmy ? cmy : cy);
+        p.x -= (float)(cx - ox) * d.cs_x;
+        p.y -= (float)(cy - oy) * d.cs_y;
+      }
+      a.posB[i] = p;
     }
-    a.posB[i] = p;
+    key = d.cell_base + local_code(d, cx, cy);
+    a.keyB[i] = key;
   }
-  a.keyB[i] = d.cell_base + local_code(d, cx, cy);
+  if (a.ghist) histogram_keys(a, hs, valid, key);
 }
 
 // ---------------------------------------------------------------- reorder + cell ranges
@@ -142,11 +150,31 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 constexpr int kForceBuf = 12;
 
 template <int PREC, bool BATCHED, int MODE>
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
+                                              uint32_t (*bj)[kThreads]);
+
+template <int PREC, bool BATCHED, int MODE>
 __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   __shared__ float2 bd[kForceBuf][kThreads];
   __shared__ uint32_t bj[kForceBuf][kThreads];
+  __shared__ uint32_t hs[4][256];
+  const bool hist = (MODE == kForceIntegrate) && a.ghist != nullptr;
+  if (hist) {
+    for (int p = 0; p < 4; ++p) hs[p][threadIdx.x] = 0;
+    __syncthreads();
+  }
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  const bool valid = i < a.n;
+  uint32_t key = 0;
+  if (valid) key = force_one<PREC, BATCHED, MODE>(a, i, bd, bj);
+  if (hist) histogram_keys(a, hs, valid, key);
+}
+
+// Forces on particle i; in integrate mode also the update and the new key
+// (returned), in force-only mode the acceleration is stored.
+template <int PREC, bool BATCHED, int MODE>
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
+                                              uint32_t (*bj)[kThreads]) {
   const InstDesc d = inst_of<BATCHED>(a, i);
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
@@ -232,9 +260,9 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   }
   if (MODE == kForceOnly) {
     a.acc[i] = make_float2(ax, ay);
-    return;
+    return 0;
   }
-  integrate_and_key<PREC>(a, d, i, cx, cy, pi, vi, ax, ay);
+  return integrate_and_key<PREC>(a, d, i, cx, cy, pi, vi, ax, ay);
 }
 
 // ---------------------------------------------------------------- diagnostics

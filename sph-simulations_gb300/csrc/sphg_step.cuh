@@ -34,6 +34,8 @@ struct StepArgs {
   uint32_t* nbr;               // [nbr_slots][n] neighbours found by the density pass: j << 5 | tag
   uint32_t* ncount;            // [n] neighbours of each particle (> nbr_slots: list overflowed)
   int nbr_slots;
+  uint32_t* ghist;             // digit histograms of the next sort (accumulated by the key writers)
+  int key_passes;              // radix passes of the next sort
   uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
   // cell tiles (Morton order only; tile_bits == 0 disables them)
   int tile_bits;               // tiles of 2^tile_bits x 2^tile_bits cells
