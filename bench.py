@@ -45,6 +45,9 @@ METRIC = ("particle-steps/s on 1 GB300, batched vs plain GPU path at ≤1e-5 rel
           "p99 latency")
 UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
+# DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
+# summed over one iteration's kernels); filled from the committed profile summaries
+TRAFFIC_PER_PARTICLE_STEP = {}
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -58,42 +61,31 @@ def peaks():
 
 
 # ---------------------------------------------------------------- workloads
-def lattice_mass(rho0, h, dx):
-    """Mass that gives rho0 on a perfect square lattice of spacing dx (2-D sum of
-    the reference's poly6 kernel, 315 / (64 pi h^9) (h^2 - r^2)^3)."""
-    s = 0.0
-    m = int(math.ceil(h / dx)) + 1
-    for i in range(-m, m + 1):
-        for j in range(-m, m + 1):
-            r2 = (i * dx) ** 2 + (j * dx) ** 2
-            if r2 <= h * h:
-                s += (h * h - r2) ** 3
-    return rho0 / (315.0 / (64.0 * math.pi * h ** 9) * s)
-
-
-def dam_break(nx, ny, dx, seed, order="morton", box=(1.0, 1.0), alpha=0.1):
-    rng = np.random.default_rng(seed)
-    gx, gy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
-    x = (gx.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
-    y = (gy.ravel() + 0.5) * dx + rng.uniform(-0.01 * dx, 0.01 * dx, gx.size)
-    h = 1.3 * dx
-    prm = dict(order=order, h=h, dt=1e-5, k=30.0, rho0=1000.0, mu=0.0, gx=0.0, gy=-9.81,
-               mass=lattice_mass(1000.0, h, dx), alpha=alpha, c0=math.sqrt(30.0),
-               lo=(0.0, 0.0), hi=box, periodic=0)
-    z = np.zeros(x.size)
-    return prm, x, y, z, z.copy()
-
+import workloads as W  # noqa: E402  (sph-simulations_gb300/workloads.py)
 
 WORKLOADS = {
-    "dam_break_1m": dict(nx=1000, ny=1000, dx=0.0005, steps_config=2000, precision="split"),
-    "dam_break_12k": dict(nx=80, ny=160, dx=0.005, steps_config=1000, precision="plain"),
+    # configs[1]: 1,000,000-particle dam break, split-precision positions (the headline)
+    "dam_break_1m": dict(kind="dam", nx=1000, ny=1000, dx=0.0005, steps_config=2000, precision="split"),
+    # configs[0]: 12,800-particle dam break, plain FP32 positions
+    "dam_break_12k": dict(kind="dam", nx=80, ny=160, dx=0.005, steps_config=1000, precision="plain"),
+    # configs[2]: periodic Taylor-Green vortex, 512 x 512
+    "tgv_262k": dict(kind="tgv", n=512, steps_config=5000, precision="plain"),
+    # configs[3]: 256 independent dam-break boxes, 2,000-65,536 particles each
+    "batch_256": dict(kind="batch", count=256, steps_config=1000, precision="split"),
 }
 
 
 def make_workload(name):
     w = WORKLOADS[name]
-    prm, x, y, vx, vy = dam_break(w["nx"], w["ny"], w["dx"], seed=0)
-    return w, prm, x, y, vx, vy
+    if w["kind"] == "dam":
+        prm, x, y, vx, vy = W.dam_break(w["nx"], w["ny"], w["dx"], seed=0)
+        return w, prm, x, y, vx, vy
+    if w["kind"] == "tgv":
+        prm, x, y, vx, vy, _ = W.taylor_green(w["n"], seed=0)
+        return w, prm, x, y, vx, vy
+    prms, counts, x, y, vx, vy = W.batch(w["count"], seed=0)
+    w = dict(w, counts=counts)
+    return w, prms, x, y, vx, vy
 
 
 # ---------------------------------------------------------------- clocks
@@ -151,29 +143,60 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle port)
-def cpu_baseline(prm, x, y, vx, vy, budget_s=15.0, max_steps=None):
+def cpu_baseline(prm, x, y, vx, vy, budget_s=15.0, max_steps=None, counts=None):
+    """The CPU restatement of the reference's OpenMP path (FP64, all host threads)
+    timed on a bounded sample of the workload: whole instances, main-loop
+    iterations until the time budget is spent."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     O.set_threads(os.cpu_count() or 1)
-    p = O.params(**prm)
-    sim = O.Sim(p, x, y, vx, vy)
-    sim.preloop()
-    t0 = time.perf_counter()
-    steps = 0
-    while True:
-        sim.steps(1)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or (max_steps and steps >= max_steps):
+    if counts is None:
+        prms, counts = [prm], [len(x)]
+    else:
+        prms = prm
+    off = np.concatenate([[0], np.cumsum(counts)])
+    done_ps, el, steps_total, insts = 0, 0.0, 0, 0
+    for k, p_k in enumerate(prms):
+        sl = slice(off[k], off[k + 1])
+        sim = O.Sim(O.params(**p_k), x[sl], y[sl], vx[sl], vy[sl])
+        sim.preloop()
+        insts += 1
+        while True:
+            t0 = time.perf_counter()
+            sim.steps(1)
+            el += time.perf_counter() - t0
+            done_ps += int(counts[k])
+            steps_total += 1
+            if el >= budget_s or (max_steps and steps_total >= max_steps * (k + 1)):
+                break
+        if el >= budget_s:
             break
-    rate = len(x) * steps / el
+    rate = done_ps / el
     return {"value": rate, "unit": UNIT, "cores": O.get_threads(), "kind": "port",
-            "sample": "%d particles, %d main-loop iterations after the pre-loop, FP64 CPU "
-                      "restatement of the reference's OpenMP path, %.1f s" % (len(x), steps, el)}
+            "sample": "%d particle-steps over %d instance(s) (%d main-loop iterations after the "
+                      "pre-loop), FP64 CPU restatement of the reference's OpenMP path, %.1f s"
+                      % (done_ps, insts, steps_total, el)}
 
 
 # ---------------------------------------------------------------- GPU arm
+def time_steps(sim, sphg, steps, stream, flush):
+    """Per-step CUDA events around each graph launch; L2 flushed between steps
+    (outside the events) when flush is not None."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    sptr = stream.cuda_stream
+    for k in range(steps):
+        if flush is not None:
+            flush.fill_(float(k))
+        ev[k][0].record(stream)
+        sim.step(1, stream=sptr)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return float(sum(a.elapsed_time(b) for a, b in ev))
+
+
 def run_gpu(args):
     import torch
     import sphg
@@ -186,37 +209,34 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     w, prm, x, y, vx, vy = make_workload(args.workload)
+    batched = w["kind"] == "batch"
     n = len(x)
     prec = sphg.SPLIT if w["precision"] == "split" else sphg.PLAIN
     opts = sphg.options(precision=prec, track_ids=0, use_graph=1)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
+    sprm = [sphg.params(**p) for p in prm] if batched else sphg.params(**prm)
 
-    # ---- device-resident timing
-    sim = sphg.Sim(sphg.params(**prm), n, opts)
+    # ---- device-resident timing (inputs in HBM; L2 flushed between steps when
+    #      the state fits in L2)
+    sim = sphg.Sim(sprm, w["counts"] if batched else n, opts)
     sim.upload(x, y, vx, vy, stream=sptr)
     sim.preloop(stream=sptr)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    state_bytes = n * 100
+    flush = None
+    if state_bytes < L2_FLUSH_BYTES:
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         sim.step(1, stream=sptr)
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    for k in range(args.steps):
-        flush.fill_(float(k))
-        ev[k][0].record(stream)
-        sim.step(1, stream=sptr)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
+    total_ms = time_steps(sim, sphg, args.steps, stream, flush)
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = float(sum(step_ms))
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -224,15 +244,46 @@ def run_gpu(args):
     ms_per_step = total_ms / args.steps
     value = n * world * args.steps / (total_ms * 1e-3)
 
-    # ---- per-phase profile (events between the kernels of one iteration)
+    # ---- per-phase profile (CUDA events between the kernels of one iteration)
     phases = np.array([sim.profile_step(stream=sptr) for _ in range(20)])
     phase_ms = phases.mean(axis=0).tolist()
-    diag = sim.diagnostics(stream=sptr)[0]
+    diag = sim.diagnostics(stream=sptr)
     launches = sim.launches_per_step() * args.steps
     sim.close()
 
+    extra = {}
+    if batched:
+        # the plain GPU path: every instance its own handle, stepped one after another
+        counts = w["counts"]
+        off = np.concatenate([[0], np.cumsum(counts)])
+        sims = []
+        for k, p_k in enumerate(prm):
+            sl = slice(off[k], off[k + 1])
+            s_k = sphg.Sim(sphg.params(**p_k), int(counts[k]), opts)
+            s_k.upload(x[sl], y[sl], vx[sl], vy[sl], stream=sptr)
+            s_k.preloop(stream=sptr)
+            sims.append(s_k)
+        psteps = max(3, min(args.steps, 20))
+        for s_k in sims:
+            s_k.step(2, stream=sptr)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(psteps):
+            for s_k in sims:
+                s_k.step(1, stream=sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain = n * psteps / (e0.elapsed_time(e1) * 1e-3)
+        for s_k in sims:
+            s_k.close()
+        extra = {"plain_gpu_path": {"value": plain, "unit": UNIT, "steps": psteps,
+                                    "how": "one handle per instance, stepped in turn"},
+                 "batched_vs_plain": value / plain}
+
     # ---- end to end through the C ABI from host buffers
-    sim = sphg.Sim(sphg.params(**prm), n, opts)
+    sim = sphg.Sim(sprm, w["counts"] if batched else n, opts)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.upload(x, y, vx, vy, stream=sptr)
@@ -243,17 +294,19 @@ def run_gpu(args):
     out = sim.download(forces=False, stream=sptr)
     e2e_s = time.perf_counter() - t0
     sim.close()
+    ninst = len(prm) if batched else 1
     e2e = {"value": n * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(n * 16 / args.steps),
-           "d2h_bytes_per_step": int(6 * 8 + n * (2 * 8 + 4 + 4 + 4) / args.steps),
+           "d2h_bytes_per_step": int(6 * 8 * ninst + n * (2 * 8 + 4 + 4 + 4) / args.steps),
            "wall_s": e2e_s}
     assert np.isfinite(out["x"]).all()
 
     hbm, src = peaks()
     achieved = value * BYTES_PER_PARTICLE_STEP / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_source": src,
-                "kernel": "one main-loop iteration (keys + radix sort + reorder + density + force)",
+                "frac": achieved / hbm, "traffic": TRAFFIC_PER_PARTICLE_STEP.get(args.workload),
+                "peak_source": src,
+                "kernel": "one main-loop iteration (radix sort + reorder + density + force)",
                 "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP}
     names = ["keys", "sort", "reorder", "density", "force_integrate"]
     tot = sum(phase_ms)
@@ -261,22 +314,34 @@ def run_gpu(args):
     dominant = max(phases_out, key=lambda k: phases_out[k]["ms"])
 
     if rank == 0:
-        cpu = cpu_baseline(prm, x, y, vx, vy, budget_s=args.cpu_budget) if args.cpu_budget > 0 else None
+        cpu = None
+        if args.cpu_budget > 0:
+            cpu = cpu_baseline(prm, x, y, vx, vy, budget_s=args.cpu_budget,
+                               counts=w["counts"] if batched else None)
+        cfg = {"workload": args.workload, "particles": n, "precision": w["precision"],
+               "steps_in_config": w["steps_config"], "replicas": "one per GPU",
+               "l2": ("flushed between timed steps (256 MiB write, outside the events)"
+                      if flush is not None else "state larger than L2 (no flush)")}
+        if batched:
+            cfg.update(instances=len(prm), physics="k=30 rho0=1000 alpha U[0.05,0.2] g=-9.81 mu=0 dt=1e-5",
+                       order="morton")
+        else:
+            cfg.update(h=prm["h"], order=prm["order"],
+                       physics="k=%g rho0=%g alpha=%g g=%g mu=%.4g dt=%g%s" % (
+                           prm["k"], prm["rho0"], prm["alpha"], prm["gy"], prm["mu"], prm["dt"],
+                           " periodic" if prm["periodic"] else ""))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded jittered-lattice dam break (no dataset)",
-            "config": {"workload": args.workload, "particles": n, "dx": w["dx"], "h": prm["h"],
-                       "order": prm["order"], "precision": w["precision"],
-                       "physics": "k=30 rho0=1000 alpha=0.1 g=-9.81 mu=0 dt=1e-5",
-                       "steps_in_config": w["steps_config"], "replicas": "one per GPU",
-                       "l2": "flushed between timed steps (256 MiB write, outside the events)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk, "phases_ms": phases_out, "dominant_phase": dominant,
-            "diagnostics_after": {"E_k": diag[0], "max_v2": diag[1], "inside": diag[2],
-                                  "nonfinite": diag[5]},
+            "data": "synthetic: seeded jittered-lattice initial states (no dataset)",
+            "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches, "clocks": clk, "phases_ms": phases_out,
+            "dominant_phase": dominant,
+            "diagnostics_after": {"E_k": float(diag[:, 0].sum()), "max_v2": float(diag[:, 1].max()),
+                                  "inside": float(diag[:, 2].sum()), "nonfinite": float(diag[:, 5].sum())},
         }
+        line.update(extra)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -287,15 +352,16 @@ def run_reference(args):
     if rank != 0:
         return
     w, prm, x, y, vx, vy = make_workload(args.workload)
+    batched = w["kind"] == "batch"
     n = len(x)
     cpu = cpu_baseline(prm, x, y, vx, vy, budget_s=args.cpu_budget if args.cpu_budget > 0 else 15.0,
-                       max_steps=max(args.steps, 1))
+                       max_steps=max(args.steps, 1), counts=w["counts"] if batched else None)
     line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT,
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded jittered-lattice dam break",
-            "config": {"workload": args.workload, "particles": n, "dx": w["dx"], "h": prm["h"],
-                       "order": prm["order"]},
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded jittered-lattice initial states (no dataset)",
+            "config": {"workload": args.workload, "particles": n},
             "cpu_baseline": cpu,
             "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}

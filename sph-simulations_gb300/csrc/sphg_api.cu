@@ -480,12 +480,12 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   auto chk = [&](cudaError_t err, const char* what) {
     if (err != cudaSuccess && st == SPHG_OK) st = fail(SPHG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
   };
+  // everything starts at zero (the step epoch, flags[2], is bumped to 1 by the
+  // first sort, so no range entry is valid before its cell is written; the
+  // table is never cleared again); then the instance descriptors
+  chk(cudaMemset(s->arena.base, 0, s->arena.size), "state init");
   chk(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice), "desc upload");
   chk(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice), "begins upload");
-  // everything starts at zero: the step epoch (flags[2]) is bumped to 1 by the
-  // first sort, so no range entry is valid before its cell is written; the
-  // table is never cleared again
-  chk(cudaMemset(s->arena.base, 0, s->arena.size), "state init");
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;

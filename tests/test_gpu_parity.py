@@ -421,3 +421,110 @@ def test_tile_overflow_falls_back_to_global_walk():
     assert rel_rho(a["rho"], rho) <= RHO_TOL
     assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
     sim.close()
+
+
+# ---------------------------------------------------------------- batches of instances
+def _instances(seed=5):
+    import workloads as W
+    rng = np.random.default_rng(seed)
+    out = []
+    for npart, aspect, alpha, order in ((900, 0.5, 0.1, "morton"), (2500, 1.7, 0.05, "morton"),
+                                        (400, 1.0, 0.2, "rowmajor"), (3000, 0.3, 0.15, "morton")):
+        prm, x, y = W.dam_break_sized(npart, aspect, 0.005, rng, alpha, order=order)
+        x = x.astype(np.float32).astype(np.float64)
+        y = y.astype(np.float32).astype(np.float64)
+        vx = rng.uniform(-0.2, 0.2, len(x)).astype(np.float32).astype(np.float64)
+        vy = rng.uniform(-0.2, 0.2, len(x)).astype(np.float32).astype(np.float64)
+        out.append((prm, x, y, vx, vy))
+    return out
+
+
+@pytest.mark.parametrize("prec", ["plain", "split"])
+def test_batch_equals_each_instance_alone(prec):
+    """Instances stepped together in one handle give each instance's result
+    alone (every per-particle computation is instance-local)."""
+    S = _sphg()
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    inst = _instances()
+    prms = [S.params(**i[0]) for i in inst]
+    counts = [len(i[1]) for i in inst]
+    cat = [np.concatenate([i[k] for i in inst]) for k in (1, 2, 3, 4)]
+    b = S.Sim(prms, counts, S.options(precision=P))
+    b.upload(*cat)
+    b.preloop()
+    b.step(30)
+    bo = b.download()
+    bd = b.diagnostics()
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for k, (prm, x, y, vx, vy) in enumerate(inst):
+        s = S.Sim(S.params(**prm), len(x), S.options(precision=P))
+        s.upload(x, y, vx, vy)
+        s.preloop()
+        s.step(30)
+        so = s.download()
+        sl = slice(off[k], off[k + 1])
+        assert (bo["ids"][sl] - off[k] == so["ids"]).all()
+        for f in ("x", "y", "vx", "vy", "rho", "fx", "fy"):
+            np.testing.assert_allclose(bo[f][sl], so[f], rtol=1e-6, atol=1e-7 * np.abs(so[f]).max())
+        np.testing.assert_allclose(bd[k], s.diagnostics()[0], rtol=1e-6)
+        s.close()
+    b.close()
+
+
+def test_batch_order_independent_bitwise():
+    """An instance gives bit-identical results whatever other instances share its batch."""
+    S = _sphg()
+    inst = _instances()
+    def run(sel):
+        prms = [S.params(**inst[i][0]) for i in sel]
+        counts = [len(inst[i][1]) for i in sel]
+        cat = [np.concatenate([inst[i][k] for i in sel]) for k in (1, 2, 3, 4)]
+        b = S.Sim(prms, counts)
+        b.upload(*cat)
+        b.preloop()
+        b.step(25)
+        o = b.download()
+        off = np.concatenate([[0], np.cumsum(counts)])
+        res = {i: {f: o[f][off[q]:off[q + 1]] for f in ("x", "y", "vx", "vy", "rho")}
+               for q, i in enumerate(sel)}
+        b.close()
+        return res
+    a = run([0, 1, 2, 3])
+    c = run([3, 1, 0])
+    for i in (0, 1, 3):
+        for f in ("x", "y", "vx", "vy", "rho"):
+            assert (a[i][f] == c[i][f]).all(), (i, f)
+
+
+# ---------------------------------------------------------------- periodic boundaries
+@pytest.mark.parametrize("prec", ["plain", "split"])
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_periodic_taylor_green_vs_oracle(prec, order):
+    S = _sphg()
+    import workloads as W
+    prm, x, y, vx, vy, rate = W.taylor_green(48, seed=2, order=order)
+    f32 = lambda a: np.asarray(a).astype(np.float32).astype(np.float64)  # noqa: E731
+    x, y, vx, vy = f32(x), f32(y), f32(vx), f32(vy)
+    p = O.params(**prm)
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    sim = S.Sim(S.params(**prm), len(x), S.options(precision=P))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    for it in range(3):
+        a = sim.download()
+        sk, s, e, rho, fx, fy = oracle_state(p, a)
+        assert (sim.debug(S.DBG_KEYS) == sk).all()
+        assert rel_rho(a["rho"], rho) <= RHO_TOL
+        assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+        offs, idx = O.neighbor_lists(p, a["x"], a["y"], sk, s, e)
+        goffs, gidx = sim.neighbor_lists()
+        assert (goffs == offs).all() and (gidx == idx).all()
+        sim.step(7)
+    # kinetic energy after the first 500 steps follows exp(-16 pi^2 nu t) closely
+    e0 = 0.5 * prm["mass"] * np.sum(vx ** 2 + vy ** 2)
+    sim.step(500 - 21)
+    d = sim.diagnostics()[0]
+    t = 500 * prm["dt"]
+    assert abs(d[0] / e0 - np.exp(-rate * t)) < 0.01
+    assert d[2] == len(x) and d[5] == 0
+    sim.close()
