@@ -347,6 +347,65 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_serve(args):
+    """configs[4]: Poisson arrivals (200/s by default) of dam-break / Taylor-Green
+    requests (50/50), 1e3-2e5 particles, 500 steps each, admitted by a fixed HBM
+    budget into one continuously batched server; requests are generated before
+    the clock starts and submitted at their arrival times."""
+    import torch
+    import sphg
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reqs = W.requests(rate=args.rate, seconds=args.serve_seconds, seed=0, steps=args.serve_steps)
+    srv = sphg.Server(args.budget_gb * 1e9, max_instances=8192,
+                      opts=sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=0))
+    stream = torch.cuda.current_stream().cuda_stream
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    pending = list(reqs)
+    ids = {}
+    lat = []
+    total_ps = 0.0
+    t0 = time.perf_counter()
+    while pending or ids:
+        now = time.perf_counter() - t0
+        while pending and pending[0][0] <= now:
+            arr, kind, prm, x, y, vx, vy, steps = pending.pop(0)
+            rid = srv.submit(sphg.params(**prm), x, y, vx, vy, steps)
+            ids[rid] = (arr, len(x) * steps)
+        live, fin = srv.tick(stream=stream)
+        if fin:
+            for rid in list(ids):
+                r = srv.result(rid)
+                if r is not None:
+                    lat.append(r["latency_s"])
+                    total_ps += ids[rid][1]
+                    del ids[rid]
+        if live == 0 and srv.stats()["queued"] == 0 and pending:
+            wait = pending[0][0] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    clk = clocks.stop()
+    lat = np.array(lat)
+    line = {
+        "metric": METRIC, "value": total_ps / wall, "unit": UNIT, "n_gpus": 1,
+        "steps": args.serve_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Poisson request stream of jittered-lattice states",
+        "config": {"workload": "serve", "rate_per_s": args.rate, "seconds": args.serve_seconds,
+                   "requests": len(reqs), "hbm_budget_gb": args.budget_gb,
+                   "particles_range": [1000, 200000], "precision": "split",
+                   "capacity_particles": st["cap_particles"], "capacity_cell_keys": st["cap_keys"]},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "max": float(lat.max()), "mean": float(lat.mean())},
+        "wall_s": wall, "ticks": st["ticks"], "device_particle_steps": st["particle_steps"],
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -373,15 +432,24 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(WORKLOADS) + ["serve"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of CPU baseline sampling (0 = skip)")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serve: arrival window")
+    ap.add_argument("--serve-steps", type=int, default=500, help="serve: steps per request")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
+        if args.workload == "serve":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference runs one simulation per process; serving has no reference counterpart"}))
+            return
         run_reference(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

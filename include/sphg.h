@@ -52,7 +52,8 @@ typedef enum sphg_status {
   SPHG_NONFINITE = 3,    /* NaN/Inf found in an input or in the state */
   SPHG_TIMEOUT = 4,      /* a bounded device wait gave up */
   SPHG_CUDA_ERROR = 5,   /* a CUDA runtime call failed */
-  SPHG_CAPACITY = 6      /* a fixed capacity (cells, particles, list entries) was exceeded */
+  SPHG_CAPACITY = 6,     /* a fixed capacity (cells, particles, list entries) was exceeded */
+  SPHG_NOT_READY = 7     /* a served request has not finished yet */
 } sphg_status;
 
 enum { SPHG_ORDER_MORTON = 0, SPHG_ORDER_ROWMAJOR = 1 };
@@ -137,6 +138,33 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
  * total in *total; offs has n+1 entries. */
 sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_t* total,
                                 void* stream);
+
+/* ---- continuous batching ("serving").  A server owns one device arena sized
+ * from an HBM budget and keeps every live simulation's state resident in it.
+ * Submitted requests queue in order; every tick admits the queue head while
+ * the live set fits the budget, runs one batched main-loop iteration of all
+ * live simulations (a newcomer's first iteration is its pre-loop), and retires
+ * the ones that ran `steps` iterations (the reference's `steps` key: the
+ * pre-loop plus steps-1 main-loop iterations).  A simulation gives the same
+ * bits whatever else is live.  No reference counterpart: the reference runs
+ * one simulation per process (app/main.cpp:20-56). */
+typedef struct sphg_server sphg_server;
+sphg_status sphg_server_create(double hbm_budget_bytes, int32_t max_instances,
+                               const sphg_options* o, sphg_server** out);
+sphg_status sphg_server_destroy(sphg_server* s);
+sphg_status sphg_server_submit(sphg_server* s, const sphg_params* p, int64_t n, const double* x,
+                               const double* y, const double* vx, const double* vy, int64_t steps,
+                               int64_t* request_id);
+/* Admit, step, retire.  *live = simulations live after the tick, *finished = retired by it. */
+sphg_status sphg_server_tick(sphg_server* s, void* stream, int32_t* live, int32_t* finished);
+/* Final state of a finished request (slot order, like sphg_download) and its
+ * latency (completion - submission, seconds); SPHG_NOT_READY until then.  The
+ * result is released once fetched. */
+sphg_status sphg_server_result(sphg_server* s, int64_t request_id, double* x, double* y, double* vx,
+                               double* vy, double* rho, int32_t* ids, double* latency_s);
+/* out[8]: live, queued, completed, particle-steps run, ticks, capacity (particles),
+ * capacity (cell keys), live particles. */
+sphg_status sphg_server_stats(sphg_server* s, double* out);
 
 /* Runs one main-loop iteration kernel by kernel with CUDA events between the
  * phases; ms[0..4] = keys, sort, reorder (+cell ranges), density, force+integrate

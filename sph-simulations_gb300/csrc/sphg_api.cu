@@ -14,13 +14,14 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sphg.h"
+#include "sphg_internal.cuh"
 #include "sphg_sort.cuh"
 #include "sphg_step.cuh"
 
 using sphg::InstDesc;
 using sphg::StepArgs;
 
-namespace {
+namespace sphg_detail {
 
 thread_local std::string g_err;
 
@@ -28,19 +29,6 @@ sphg_status fail(sphg_status st, const std::string& msg) {
   g_err = msg;
   return st;
 }
-
-#define SPHG_CUDA(expr)                                                                   \
-  do {                                                                                    \
-    cudaError_t e_ = (expr);                                                              \
-    if (e_ != cudaSuccess)                                                                \
-      return fail(SPHG_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_));  \
-  } while (0)
-
-#define SPHG_TRY(expr)                   \
-  do {                                   \
-    sphg_status st_ = (expr);            \
-    if (st_ != SPHG_OK) return st_;      \
-  } while (0)
 
 int next_pow2(int n) {
   int p = 1;
@@ -177,96 +165,15 @@ int host_cell(double x, double lo, double cs, int cmax) {
   return (int)q;
 }
 
-struct Arena {
-  char* base = nullptr;
-  size_t size = 0, used = 0;
-  template <class T>
-  T* take(size_t count) {
-    size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
-    T* p = reinterpret_cast<T*>(base + used);
-    used += bytes;
-    return p;
-  }
-};
 
-}  // namespace
+}  // namespace sphg_detail
 
 namespace sphg {
-void set_last_error(const std::string& msg) { g_err = msg; }
+void set_last_error(const std::string& msg) { sphg_detail::g_err = msg; }
 }  // namespace sphg
 
-struct sphg_sim {
-  int ninst = 0;
-  int64_t n = 0;
-  sphg_options opt{};
-  std::vector<sphg_params> params;
-  std::vector<int64_t> counts;
-  std::vector<InstDesc> hdesc;
-  std::vector<int32_t> hbegins;
-  uint64_t total_keys = 0;
-  int key_bits = 1;
-  int diag_chunks = 1;
-  Arena arena;
-  // device buffers
-  InstDesc* ddesc = nullptr;
-  int32_t* dbegins = nullptr;
-  float2 *posA = nullptr, *posB = nullptr, *velB = nullptr, *acc = nullptr;
-  float4* velpA = nullptr;
-  float* rho = nullptr;
-  uint32_t *keyA = nullptr, *keyB = nullptr, *keyTmp = nullptr, *perm = nullptr,
-           *valTmp = nullptr, *scratch = nullptr, *flags = nullptr;
-  uint4* ranges = nullptr;
-  int32_t *idsA = nullptr, *idsB = nullptr;
-  double *diag_partials = nullptr, *diag_out = nullptr;
-  uint2* tile_ranges = nullptr;
-  uint32_t* tile_list = nullptr;
-  uint32_t *nbr = nullptr, *ncount = nullptr;
-  int nbr_slots = 0;
-  int tile_bits = 0, tile_cap = 0, tile_grid = 0;
-  bool uploaded = false, preloop_done = false;
-  // CUDA graph of one step
-  cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t gexec = nullptr;
 
-  StepArgs args() const {
-    StepArgs a;
-    std::memset(&a, 0, sizeof(a));
-    a.n = n;
-    a.ninst = ninst;
-    a.track_ids = opt.track_ids;
-    a.d0 = hdesc[0];
-    a.desc = ddesc;
-    a.begins = dbegins;
-    a.posA = posA;
-    a.velpA = velpA;
-    a.rho = rho;
-    a.keyA = keyA;
-    a.ranges = ranges;
-    a.epoch = flags + 2;
-    a.idsA = idsA;
-    a.posB = posB;
-    a.velB = velB;
-    a.keyB = keyB;
-    a.idsB = idsB;
-    a.perm = perm;
-    a.acc = acc;
-    a.flags = flags;
-    a.tile_bits = tile_bits;
-    a.tile_cap = tile_cap;
-    a.tile_grid = tile_grid;
-    a.tile_ranges = tile_ranges;
-    a.tile_list = tile_list;
-    a.tile_count = flags + 1;
-    a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
-    a.ghist = nullptr;  // the sort computes its digit histograms itself
-    a.key_passes = (key_bits + 7) / 8;
-    a.ncount = ncount;
-    a.nbr_slots = nbr_slots;
-    return a;
-  }
-};
-
-namespace {
+namespace sphg_detail {
 
 // One main-loop iteration.  The force kernel writes the keys of the integrated
 // state, so the key pass only runs on the first iteration after an upload.
@@ -323,6 +230,140 @@ sphg_status run_steps(sphg_sim* s, int64_t k, cudaStream_t st, bool first = fals
   return SPHG_OK;
 }
 
+
+// Options shared by every handle: precision mode, cell tiles (Morton only).
+sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p) {
+  if (s->opt.precision != SPHG_PRECISION_PLAIN && s->opt.precision != SPHG_PRECISION_SPLIT)
+    return fail(SPHG_INVALID_ARG, "unknown precision mode");
+  bool all_morton = true;
+  for (int i = 0; i < ninst; ++i) all_morton = all_morton && p[i].order == SPHG_ORDER_MORTON;
+  int tb = s->opt.tile_bits;
+  if (tb == 0) tb = -1;  // default: one thread per particle (faster than the tiles at these densities)
+  if (tb > 0 && (!all_morton || tb < 3 || tb > 5))
+    return fail(SPHG_INVALID_ARG, "cell tiles need Morton order on every instance and tile_bits in 3..5");
+  s->tile_bits = tb > 0 ? tb : 0;
+  return SPHG_OK;
+}
+
+// Descriptors of ninst instances laid out one after the other; cell keys of
+// instance i start at the sum of the previous spans (rounded to a tile block
+// when tiles are on, so no tile spans two instances).  keys_cap > 0 bounds the
+// key space.
+sphg_status compute_layout(sphg_sim* s, int ninst, const sphg_params* p, const int64_t* counts,
+                           uint64_t keys_cap, Layout& L) {
+  const uint64_t key_align = s->tile_bits ? ((uint64_t)1 << (2 * 5)) : 1;
+  L.desc.assign(ninst, InstDesc());
+  L.begins.assign(ninst, 0);
+  L.n = 0;
+  L.keys = 0;
+  L.max_n = 0;
+  for (int i = 0; i < ninst; ++i) {
+    if (counts[i] < 0) return fail(SPHG_INVALID_ARG, "negative particle count");
+    uint64_t span = 0;
+    SPHG_TRY(make_desc(p[i], L.n, counts[i], L.keys, L.desc[i], span));
+    L.begins[i] = (int32_t)L.n;
+    L.n += counts[i];
+    L.keys += (span + key_align - 1) / key_align * key_align;
+    L.max_n = std::max(L.max_n, counts[i]);
+    if (L.n >= (int64_t)0x7fffffff || L.keys >= (uint64_t)0xfffffff0u)
+      return fail(SPHG_CAPACITY, "more than 2^31 particles or 2^32 cell keys in one handle");
+  }
+  if (keys_cap && L.keys > keys_cap) return fail(SPHG_CAPACITY, "cell keys exceed the handle's key capacity");
+  return SPHG_OK;
+}
+
+// One device arena sized for N particles, `keys` cell keys and ninst instances.
+sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int diag_chunks) {
+  s->cap_n = N;
+  s->cap_keys = keys;
+  s->cap_inst = ninst;
+  s->diag_chunks = diag_chunks;
+  // per-particle neighbour slots filled by the density pass and read by the
+  // force pass (indices are packed as j << 5, so only below 2^27 particles)
+  s->nbr_slots = (N < ((size_t)1 << 27)) ? 12 : 0;
+  auto layout = [&](Arena& A) {
+    s->ddesc = A.take<InstDesc>(ninst);
+    s->dbegins = A.take<int32_t>(ninst);
+    s->posA = A.take<float2>(N);
+    s->posB = A.take<float2>(N);
+    s->velB = A.take<float2>(N);
+    s->acc = A.take<float2>(N);
+    s->velpA = A.take<float4>(N);
+    s->rho = A.take<float>(N);
+    s->keyA = A.take<uint32_t>(N);
+    s->keyB = A.take<uint32_t>(N);
+    s->keyTmp = A.take<uint32_t>(N);
+    s->perm = A.take<uint32_t>(N);
+    s->valTmp = A.take<uint32_t>(N);
+    s->scratch = A.take<uint32_t>(sphg::sort_scratch_words(N));
+    s->flags = A.take<uint32_t>(16);
+    s->diag_partials = A.take<double>((size_t)ninst * s->diag_chunks * 6);
+    s->diag_out = A.take<double>((size_t)ninst * 6);
+    if (s->opt.track_ids) {
+      s->idsA = A.take<int32_t>(N);
+      s->idsB = A.take<int32_t>(N);
+    }
+    if (s->nbr_slots) {
+      s->nbr = A.take<uint32_t>(N * (size_t)s->nbr_slots);
+      s->ncount = A.take<uint32_t>(N);
+    }
+    if (s->tile_bits) {
+      s->tile_ranges = A.take<uint2>((keys >> (2 * s->tile_bits)) + 1);
+      s->tile_list = A.take<uint32_t>(std::min<uint64_t>(N, (keys >> (2 * s->tile_bits)) + 1));
+    }
+    s->ranges = A.take<uint4>(std::max<uint64_t>(keys, 1));
+  };
+  if (s->tile_bits) {
+    const int fw = (1 << s->tile_bits) + 2;
+    s->tile_cap = (3 * fw * fw + 127) / 128 * 128;
+    const uint64_t max_tiles = std::min<uint64_t>(N, (keys >> (2 * s->tile_bits)) + 1);
+    s->tile_grid = (int)std::min<uint64_t>(max_tiles, 4096);
+  }
+  Arena probe;
+  layout(probe);
+  cudaError_t e = cudaMalloc(&s->arena.base, probe.used);
+  if (e != cudaSuccess)
+    return fail(SPHG_OOM, std::string("cudaMalloc of the state arena failed: ") + cudaGetErrorString(e));
+  s->arena.size = probe.used;
+  layout(s->arena);
+  // everything starts at zero: the step epoch (flags[2]) is bumped to 1 by the
+  // first sort, so no range entry is valid before its cell is written; the
+  // table is never cleared again
+  e = cudaMemset(s->arena.base, 0, s->arena.size);
+  if (e != cudaSuccess) return fail(SPHG_CUDA_ERROR, std::string("state init: ") + cudaGetErrorString(e));
+  return SPHG_OK;
+}
+
+// Makes layout L current: host copies, key bits, descriptors on the device
+// (stream-ordered when stream is given, else synchronous).
+sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int64_t* counts,
+                         const Layout& L, cudaStream_t* stream) {
+  if (ninst > s->cap_inst || (size_t)L.n > s->cap_n || L.keys > std::max<uint64_t>(s->cap_keys, 1))
+    return fail(SPHG_CAPACITY, "layout exceeds the handle's capacity");
+  s->ninst = ninst;
+  s->params.assign(p, p + ninst);
+  s->counts.assign(counts, counts + ninst);
+  s->hdesc = L.desc;
+  s->hbegins = L.begins;
+  s->n = L.n;
+  s->total_keys = L.keys;
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) < L.keys) ++bits;
+  s->key_bits = bits;
+  if (s->gexec) {  // grid sizes depend on the layout
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+  }
+  if (stream) {
+    SPHG_CUDA(cudaMemcpyAsync(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice, *stream));
+    SPHG_CUDA(cudaMemcpyAsync(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice, *stream));
+  } else {
+    SPHG_CUDA(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice));
+    SPHG_CUDA(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice));
+  }
+  return SPHG_OK;
+}
+
 sphg_status destroy_impl(sphg_sim* s) {
   if (!s) return SPHG_OK;
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
@@ -332,7 +373,9 @@ sphg_status destroy_impl(sphg_sim* s) {
   return SPHG_OK;
 }
 
-}  // namespace
+}  // namespace sphg_detail
+
+using namespace sphg_detail;
 
 extern "C" {
 
@@ -375,117 +418,23 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   *out = nullptr;
   sphg_sim* s = new sphg_sim();
   if (o) s->opt = *o; else sphg_default_options(&s->opt);
-  if (s->opt.precision != SPHG_PRECISION_PLAIN && s->opt.precision != SPHG_PRECISION_SPLIT) {
+  sphg_status st = check_options(s, ninst, p);
+  if (st != SPHG_OK) {
     delete s;
-    return fail(SPHG_INVALID_ARG, "unknown precision mode");
+    return st;
   }
-  s->ninst = ninst;
-  s->params.assign(p, p + ninst);
-  s->counts.assign(counts, counts + ninst);
-  s->hdesc.resize(ninst);
-  s->hbegins.resize(ninst);
-  bool all_morton = true;
-  for (int i = 0; i < ninst; ++i) all_morton = all_morton && p[i].order == SPHG_ORDER_MORTON;
-  int tb = s->opt.tile_bits;
-  if (tb == 0) tb = -1;  // default: one thread per particle (faster than the tiles at these densities)
-  if (tb > 0 && (!all_morton || tb < 3 || tb > 5)) {
+  Layout L;
+  st = compute_layout(s, ninst, p, counts, 0, L);
+  if (st != SPHG_OK) {
     delete s;
-    return fail(SPHG_INVALID_ARG, "cell tiles need Morton order on every instance and tile_bits in 3..5");
+    return st;
   }
-  s->tile_bits = tb > 0 ? tb : 0;
-  // instances start on a tile boundary of the key space so no tile spans two instances
-  const uint64_t key_align = s->tile_bits ? ((uint64_t)1 << (2 * 5)) : 1;
-  int64_t begin = 0, max_n = 0;
-  uint64_t base = 0;
-  for (int i = 0; i < ninst; ++i) {
-    if (counts[i] < 0) {
-      delete s;
-      return fail(SPHG_INVALID_ARG, "negative particle count");
-    }
-    uint64_t span = 0;
-    sphg_status st = make_desc(p[i], begin, counts[i], base, s->hdesc[i], span);
-    if (st != SPHG_OK) {
-      delete s;
-      return st;
-    }
-    s->hbegins[i] = (int32_t)begin;
-    begin += counts[i];
-    base += (span + key_align - 1) / key_align * key_align;
-    max_n = std::max(max_n, counts[i]);
-    if (begin >= (int64_t)0x7fffffff || base >= (uint64_t)0xfffffff0u) {
-      delete s;
-      return fail(SPHG_CAPACITY, "more than 2^31 particles or 2^32 cell keys in one handle");
-    }
-  }
-  s->n = begin;
-  s->total_keys = base;
-  int bits = 1;
-  while (bits < 32 && ((uint64_t)1 << bits) < base) ++bits;
-  s->key_bits = bits;
-  s->diag_chunks = sphg::diag_chunks(max_n);
-
-  const size_t N = (size_t)std::max<int64_t>(s->n, 1);
-  // per-particle neighbour slots filled by the density pass and read by the
-  // force pass (indices are packed as j << 5, so only below 2^27 particles)
-  s->nbr_slots = (s->n < ((int64_t)1 << 27)) ? 12 : 0;
-  // one layout function for the size probe and the real carve-up
-  auto layout = [&](Arena& A) {
-    s->ddesc = A.take<InstDesc>(ninst);
-    s->dbegins = A.take<int32_t>(ninst);
-    s->posA = A.take<float2>(N);
-    s->posB = A.take<float2>(N);
-    s->velB = A.take<float2>(N);
-    s->acc = A.take<float2>(N);
-    s->velpA = A.take<float4>(N);
-    s->rho = A.take<float>(N);
-    s->keyA = A.take<uint32_t>(N);
-    s->keyB = A.take<uint32_t>(N);
-    s->keyTmp = A.take<uint32_t>(N);
-    s->perm = A.take<uint32_t>(N);
-    s->valTmp = A.take<uint32_t>(N);
-    s->scratch = A.take<uint32_t>(sphg::sort_scratch_words(N));
-    s->flags = A.take<uint32_t>(16);
-    s->diag_partials = A.take<double>((size_t)ninst * s->diag_chunks * 6);
-    s->diag_out = A.take<double>((size_t)ninst * 6);
-    if (s->opt.track_ids) {
-      s->idsA = A.take<int32_t>(N);
-      s->idsB = A.take<int32_t>(N);
-    }
-    if (s->nbr_slots) {
-      s->nbr = A.take<uint32_t>(N * (size_t)s->nbr_slots);
-      s->ncount = A.take<uint32_t>(N);
-    }
-    if (s->tile_bits) {
-      s->tile_ranges = A.take<uint2>((base >> (2 * s->tile_bits)) + 1);
-      s->tile_list = A.take<uint32_t>(std::min<uint64_t>(N, (base >> (2 * s->tile_bits)) + 1));
-    }
-    s->ranges = A.take<uint4>(std::max<uint64_t>(base, 1));
-  };
-  if (s->tile_bits) {
-    const int fw = (1 << s->tile_bits) + 2;
-    s->tile_cap = (3 * fw * fw + 127) / 128 * 128;
-    const uint64_t max_tiles = std::min<uint64_t>(N, (base >> (2 * s->tile_bits)) + 1);
-    s->tile_grid = (int)std::min<uint64_t>(max_tiles, 4096);
-  }
-  Arena probe;
-  layout(probe);
-  cudaError_t e = cudaMalloc(&s->arena.base, probe.used);
-  if (e != cudaSuccess) {
+  st = alloc_arena(s, (size_t)std::max<int64_t>(L.n, 1), L.keys, ninst, sphg::diag_chunks(L.max_n));
+  if (st != SPHG_OK) {
     delete s;
-    return fail(SPHG_OOM, std::string("cudaMalloc of the state arena failed: ") + cudaGetErrorString(e));
+    return st;
   }
-  s->arena.size = probe.used;
-  layout(s->arena);
-  sphg_status st = SPHG_OK;
-  auto chk = [&](cudaError_t err, const char* what) {
-    if (err != cudaSuccess && st == SPHG_OK) st = fail(SPHG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
-  };
-  // everything starts at zero (the step epoch, flags[2], is bumped to 1 by the
-  // first sort, so no range entry is valid before its cell is written; the
-  // table is never cleared again); then the instance descriptors
-  chk(cudaMemset(s->arena.base, 0, s->arena.size), "state init");
-  chk(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice), "desc upload");
-  chk(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice), "begins upload");
+  st = apply_layout(s, ninst, p, counts, L, nullptr);
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;

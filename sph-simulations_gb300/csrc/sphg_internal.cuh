@@ -1,0 +1,148 @@
+// sphg_internal.cuh -- the handle behind the C ABI, shared by sphg_api.cu
+// (single instances and fixed batches) and sphg_server.cu (continuous batching).
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sphg.h"
+#include "sphg_step.cuh"
+
+using sphg::InstDesc;
+using sphg::StepArgs;
+
+namespace sphg_detail {
+
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  template <class T>
+  T* take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+}  // namespace sphg_detail
+
+struct sphg_sim {
+  int ninst = 0;
+  int64_t n = 0;
+  sphg_options opt{};
+  std::vector<sphg_params> params;
+  std::vector<int64_t> counts;
+  std::vector<InstDesc> hdesc;
+  std::vector<int32_t> hbegins;
+  uint64_t total_keys = 0;
+  int key_bits = 1;
+  int diag_chunks = 1;
+  sphg_detail::Arena arena;
+  // device buffers
+  InstDesc* ddesc = nullptr;
+  int32_t* dbegins = nullptr;
+  float2 *posA = nullptr, *posB = nullptr, *velB = nullptr, *acc = nullptr;
+  float4* velpA = nullptr;
+  float* rho = nullptr;
+  uint32_t *keyA = nullptr, *keyB = nullptr, *keyTmp = nullptr, *perm = nullptr,
+           *valTmp = nullptr, *scratch = nullptr, *flags = nullptr;
+  uint4* ranges = nullptr;
+  int32_t *idsA = nullptr, *idsB = nullptr;
+  double *diag_partials = nullptr, *diag_out = nullptr;
+  uint2* tile_ranges = nullptr;
+  uint32_t* tile_list = nullptr;
+  uint32_t *nbr = nullptr, *ncount = nullptr;
+  int nbr_slots = 0;
+  size_t cap_n = 0;             // arena capacity (particles)
+  uint64_t cap_keys = 0;        // arena capacity (cell keys)
+  int cap_inst = 0;             // arena capacity (instances)
+  int force_batched = 0;        // always use the per-instance-descriptor kernels
+  int tile_bits = 0, tile_cap = 0, tile_grid = 0;
+  bool uploaded = false, preloop_done = false;
+  // CUDA graph of one step
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+
+  StepArgs args() const {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = n;
+    a.ninst = ninst;
+    a.track_ids = opt.track_ids;
+    if (!hdesc.empty()) a.d0 = hdesc[0];
+    a.desc = ddesc;
+    a.begins = dbegins;
+    a.posA = posA;
+    a.velpA = velpA;
+    a.rho = rho;
+    a.keyA = keyA;
+    a.ranges = ranges;
+    a.epoch = flags + 2;
+    a.idsA = idsA;
+    a.posB = posB;
+    a.velB = velB;
+    a.keyB = keyB;
+    a.idsB = idsB;
+    a.perm = perm;
+    a.acc = acc;
+    a.flags = flags;
+    a.tile_bits = tile_bits;
+    a.tile_cap = tile_cap;
+    a.tile_grid = tile_grid;
+    a.tile_ranges = tile_ranges;
+    a.tile_list = tile_list;
+    a.tile_count = flags + 1;
+    a.force_batched = force_batched;
+    a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
+    a.ghist = nullptr;  // the sort computes its digit histograms itself
+    a.key_passes = (key_bits + 7) / 8;
+    a.ncount = ncount;
+    a.nbr_slots = nbr_slots;
+    return a;
+  }
+};
+
+namespace sphg_detail {
+
+sphg_status fail(sphg_status st, const std::string& msg);
+
+#define SPHG_CUDA(expr)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(SPHG_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+#define SPHG_TRY(expr)                   \
+  do {                                   \
+    sphg_status st_ = (expr);            \
+    if (st_ != SPHG_OK) return st_;      \
+  } while (0)
+
+
+sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64_t cell_base,
+                      InstDesc& d, uint64_t& span);
+int host_cell(double x, double lo, double cs, int cmax);
+uint32_t morton_host(uint32_t x, uint32_t y);
+void demorton_host(uint32_t z, int& x, int& y);
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first);
+
+struct Layout {
+  std::vector<InstDesc> desc;
+  std::vector<int32_t> begins;
+  int64_t n = 0, max_n = 0;
+  uint64_t keys = 0;
+};
+sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p);
+sphg_status compute_layout(sphg_sim* s, int ninst, const sphg_params* p, const int64_t* counts,
+                           uint64_t keys_cap, Layout& L);
+sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int diag_chunks);
+sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int64_t* counts,
+                         const Layout& L, cudaStream_t* stream);
+sphg_status destroy_impl(sphg_sim* s);
+
+}  // namespace sphg_detail

@@ -151,7 +151,7 @@ int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, in
             ck(cudaMallocAsync((void**)&doffs, (n + 1) * sizeof(int64_t), st), "cudaMallocAsync") &&
             ck(cudaMallocAsync((void**)&dsums, (ntiles + 1) * sizeof(int64_t), st), "cudaMallocAsync");
   if (!ok) { cleanup(); return SPHG_OOM; }
-  const bool batched = a.ninst > 1;
+  const bool batched = (a.ninst > 1 || a.force_batched);
   if (precision) {
     if (batched) lists_count<1, true><<<g, kListThreads, 0, st>>>(a, dcounts);
     else lists_count<1, false><<<g, kListThreads, 0, st>>>(a, dcounts);

@@ -370,7 +370,7 @@ static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t -
 cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
-  SPHG_DISPATCH2(precision, a.ninst > 1, step_keys);
+  SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_keys);
   return cudaGetLastError();
 }
 
@@ -383,15 +383,15 @@ cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
 cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
-  SPHG_DISPATCH2(precision, a.ninst > 1, step_density);
+  SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_density);
   return cudaGetLastError();
 }
 
 cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
-  if (mode == kForceOnly) SPHG_DISPATCH2(precision, a.ninst > 1, step_force, , kForceOnly);
-  else SPHG_DISPATCH2(precision, a.ninst > 1, step_force, , kForceIntegrate);
+  if (mode == kForceOnly) SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_force, , kForceOnly);
+  else SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_force, , kForceIntegrate);
   return cudaGetLastError();
 }
 

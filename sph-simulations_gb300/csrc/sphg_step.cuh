@@ -13,6 +13,7 @@ struct StepArgs {
   int64_t n;
   int ninst;
   int track_ids;
+  int force_batched;           // 1: per-instance descriptor kernels even for one instance
   InstDesc d0;                 // copy of desc[0] (single-instance fast path)
   const InstDesc* desc;        // [ninst]
   const int32_t* begins;       // [ninst]

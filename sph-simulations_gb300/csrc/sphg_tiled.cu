@@ -285,7 +285,7 @@ static cudaError_t launch_tiles_t(const StepArgs& a, cudaStream_t s) {
 
 template <bool FORCE, int TB>
 static cudaError_t launch_tiles_tb(const StepArgs& a, int precision, cudaStream_t s) {
-  const bool b = a.ninst > 1;
+  const bool b = (a.ninst > 1 || a.force_batched);
   if (precision) return b ? launch_tiles_t<1, true, FORCE, TB>(a, s) : launch_tiles_t<1, false, FORCE, TB>(a, s);
   return b ? launch_tiles_t<0, true, FORCE, TB>(a, s) : launch_tiles_t<0, false, FORCE, TB>(a, s);
 }

@@ -14,7 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsphg.so")
 
-OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY = range(7)
+OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY, NOT_READY = range(8)
 ORDER = {"morton": 0, "rowmajor": 1}
 PLAIN, SPLIT = 0, 1
 DBG_KEYS, DBG_PERM, DBG_UNSORTED_KEYS, DBG_POS_NEXT, DBG_VEL_NEXT = range(5)
@@ -78,6 +78,15 @@ def lib():
         L.sphg_profile_step.restype = ctypes.c_int
         L.sphg_launches_per_step.argtypes = [SP]
         L.sphg_launches_per_step.restype = ctypes.c_int32
+        L.sphg_server_create.argtypes = [ctypes.c_double, ctypes.c_int32, OP, ctypes.POINTER(SP)]
+        L.sphg_server_destroy.argtypes = [SP]
+        L.sphg_server_submit.argtypes = [SP, PP, ctypes.c_int64, _dp, _dp, _dp, _dp, ctypes.c_int64, _lp]
+        L.sphg_server_tick.argtypes = [SP, _vp, _ip, _ip]
+        L.sphg_server_result.argtypes = [SP, ctypes.c_int64] + [_dp] * 5 + [_ip, _dp]
+        L.sphg_server_stats.argtypes = [SP, _dp]
+        for f in ("sphg_server_create", "sphg_server_destroy", "sphg_server_submit",
+                  "sphg_server_tick", "sphg_server_result", "sphg_server_stats"):
+            getattr(L, f).restype = ctypes.c_int
         L.sphg_sort_pairs.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp]
         L.sphg_cell_keys.argtypes = [PP, _vp, _vp, ctypes.c_int64, _vp, _vp]
         for f in ("sphg_create", "sphg_create_batch", "sphg_destroy", "sphg_upload",
@@ -219,6 +228,66 @@ class Sim:
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().sphg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous batching of independent simulations (sphg_server_*)."""
+
+    def __init__(self, budget_bytes, max_instances=4096, opts=None):
+        self._h = ctypes.c_void_p()
+        self.opts = opts if opts is not None else options()
+        check(lib().sphg_server_create(float(budget_bytes), int(max_instances),
+                                       ctypes.byref(self.opts), ctypes.byref(self._h)))
+        self.sizes = {}
+
+    def submit(self, prm, x, y, vx, vy, steps):
+        x, y, vx, vy = _f64(x), _f64(y), _f64(vx), _f64(vy)
+        rid = ctypes.c_int64(0)
+        check(lib().sphg_server_submit(self._h, ctypes.byref(prm), len(x), _ptr(x), _ptr(y),
+                                       _ptr(vx), _ptr(vy), int(steps), ctypes.byref(rid)))
+        self.sizes[rid.value] = len(x)
+        return rid.value
+
+    def tick(self, stream=None):
+        live = ctypes.c_int32(0)
+        fin = ctypes.c_int32(0)
+        check(lib().sphg_server_tick(self._h, _stream(stream), ctypes.byref(live), ctypes.byref(fin)))
+        return live.value, fin.value
+
+    def result(self, rid):
+        """dict of the final state and latency, or None while the request runs."""
+        n = self.sizes[rid]
+        out = {k: np.empty(n, np.float64) for k in ("x", "y", "vx", "vy", "rho")}
+        ids = np.empty(n, np.int32)
+        lat = ctypes.c_double(0)
+        st = lib().sphg_server_result(self._h, rid, _ptr(out["x"]), _ptr(out["y"]), _ptr(out["vx"]),
+                                      _ptr(out["vy"]), _ptr(out["rho"]), _ptr(ids, _ip),
+                                      ctypes.byref(lat))
+        if st == NOT_READY:
+            return None
+        check(st)
+        out["ids"] = ids
+        out["latency_s"] = lat.value
+        del self.sizes[rid]
+        return out
+
+    def stats(self):
+        out = np.zeros(8, np.float64)
+        check(lib().sphg_server_stats(self._h, _ptr(out)))
+        keys = ("live", "queued", "completed", "particle_steps", "ticks", "cap_particles",
+                "cap_keys", "live_particles")
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sphg_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

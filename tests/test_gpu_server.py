@@ -1,0 +1,111 @@
+"""Continuous batching (sphg_server_*): results are the same alone and in the
+mix, admission respects the capacity, latency is reported."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(seed, count):
+    import workloads as W
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        if k % 2 == 0:
+            npart = int(rng.integers(300, 3000))
+            prm, x, y = W.dam_break_sized(npart, rng.uniform(0.3, 2.0), 0.005, rng, alpha=0.1)
+            vx = np.zeros(len(x))
+            vy = np.zeros(len(x))
+        else:
+            prm, x, y, vx, vy, _ = W.taylor_green(int(rng.integers(12, 40)), seed=int(rng.integers(1 << 20)))
+        out.append((prm, x, y, vx, vy, int(rng.integers(5, 25))))
+    return out
+
+
+def _serve(S, reqs, budget=2e9, stagger=True):
+    srv = S.Server(budget)
+    ids = []
+    pending = list(reqs)
+    results = {}
+    while pending or len(results) < len(reqs):
+        # submit a couple of requests per tick so arrivals overlap running work
+        for _ in range(2 if stagger else len(pending)):
+            if pending:
+                prm, x, y, vx, vy, steps = pending.pop(0)
+                ids.append(srv.submit(S.params(**prm), x, y, vx, vy, steps))
+        srv.tick()
+        for rid in ids:
+            if rid not in results:
+                r = srv.result(rid)
+                if r is not None:
+                    results[rid] = r
+    stats = srv.stats()
+    srv.close()
+    return [results[i] for i in ids], stats
+
+
+def test_served_results_equal_alone_and_in_the_mix():
+    import sphg as S
+    reqs = _requests(1, 10)
+    mixed, stats = _serve(S, reqs)
+    assert stats["completed"] == len(reqs) and stats["live"] == 0
+    for k, req in enumerate(reqs):
+        alone, _ = _serve(S, [req])
+        for f in ("x", "y", "vx", "vy", "rho"):
+            assert (alone[0][f] == mixed[k][f]).all(), (k, f)  # same bits
+        assert mixed[k]["latency_s"] > 0
+        # and the same state as a plain single-instance handle run (pre-loop + steps-1)
+        prm, x, y, vx, vy, steps = req
+        sim = S.Sim(S.params(**prm), len(x))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        sim.step(steps - 1)
+        o = sim.download(forces=False)
+        sim.close()
+        assert (o["ids"] == mixed[k]["ids"]).all()
+        for f in ("x", "y", "vx", "vy", "rho"):
+            np.testing.assert_allclose(mixed[k][f], o[f], rtol=1e-6, atol=1e-7 * np.abs(o[f]).max())
+
+
+def test_admission_respects_capacity_fifo():
+    import sphg as S
+    reqs = _requests(2, 8)
+    # a budget for ~6,000 particles (160 B/particle for state, the rest for cell keys)
+    budget = 2 * 160.0 * 6000
+    srv = S.Server(budget)
+    cap = srv.stats()["cap_particles"]
+    ids = [srv.submit(S.params(**r[0]), *r[1:5], r[5]) for r in reqs if len(r[1]) <= cap]
+    done = {}
+    order = []
+    max_live_particles = 0
+    for _ in range(10000):
+        srv.tick()
+        st = srv.stats()
+        max_live_particles = max(max_live_particles, st["live_particles"])
+        for rid in ids:
+            if rid not in done:
+                r = srv.result(rid)
+                if r is not None:
+                    done[rid] = r
+                    order.append(rid)
+        if len(done) == len(ids):
+            break
+    assert len(done) == len(ids)
+    assert max_live_particles <= cap
+    srv.close()
+
+
+def test_server_rejects_bad_requests():
+    import sphg as S
+    srv = S.Server(1e6)
+    prm = S.params(h=0.01, lo=(0, 0), hi=(1, 1))
+    with pytest.raises(S.SphgError):
+        srv.submit(prm, [0.5], [0.5], [0.0], [0.0], 0)  # steps < 1
+    with pytest.raises(S.SphgError) as ei:
+        srv.submit(prm, [0.5, np.inf], [0.5, 0.5], [0, 0], [0, 0], 3)
+    assert ei.value.status == S.NONFINITE
+    big = np.linspace(0.1, 0.9, 100000)
+    with pytest.raises(S.SphgError) as ei:
+        srv.submit(prm, big, big, big * 0, big * 0, 3)
+    assert ei.value.status == S.CAPACITY
+    srv.close()
