@@ -139,6 +139,14 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
 sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_t* total,
                                 void* stream);
 
+/* Binary snapshot of the current state in the device representation (positions
+ * or split cell + offset, velocities, cell keys, creation indices) so a run can
+ * resume exactly: sphg_restore + sphg_preloop continues bit for bit where the
+ * snapshot was taken.  buf == NULL: *bytes receives the size.  No reference
+ * counterpart (CheckPointWriter writes positions only, core/utils/CheckPointWriter.cpp:11-27). */
+sphg_status sphg_snapshot(sphg_sim* s, void* buf, uint64_t* bytes, void* stream);
+sphg_status sphg_restore(sphg_sim* s, const void* buf, uint64_t bytes, void* stream);
+
 /* ---- continuous batching ("serving").  A server owns one device arena sized
  * from an HBM budget and keeps every live simulation's state resident in it.
  * Submitted requests queue in order; every tick admits the queue head while

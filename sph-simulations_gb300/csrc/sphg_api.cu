@@ -640,6 +640,82 @@ sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_
   return SPHG_OK;
 }
 
+namespace {
+struct SnapHeader {
+  uint64_t magic;       // "SPHGSNAP"
+  uint32_t version, precision;
+  int64_t n;
+  int32_t ninst, track_ids;
+};
+constexpr uint64_t kSnapMagic = 0x50414e5347485053ull;
+}  // namespace
+
+sphg_status sphg_snapshot(sphg_sim* s, void* buf, uint64_t* bytes, void* stream) {
+  if (!s || !bytes) return fail(SPHG_INVALID_ARG, "null argument");
+  if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state to snapshot");
+  const int64_t n = s->n;
+  const uint64_t need = sizeof(SnapHeader) + (uint64_t)n * (sizeof(float2) * 2 + sizeof(uint32_t) + sizeof(int32_t));
+  if (!buf) {
+    *bytes = need;
+    return SPHG_OK;
+  }
+  if (*bytes < need) return fail(SPHG_INVALID_ARG, "snapshot buffer too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  SnapHeader h{kSnapMagic, 1u, (uint32_t)s->opt.precision, n, s->ninst, s->opt.track_ids};
+  char* p = static_cast<char*>(buf);
+  std::memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  float2* pos = reinterpret_cast<float2*>(p);
+  float2* vel = pos + n;
+  uint32_t* key = reinterpret_cast<uint32_t*>(vel + n);
+  int32_t* ids = reinterpret_cast<int32_t*>(key + n);
+  if (n > 0) {
+    std::vector<float4> velp(n);
+    SPHG_CUDA(cudaMemcpyAsync(pos, s->posA, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaMemcpyAsync(velp.data(), s->velpA, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaMemcpyAsync(key, s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (s->opt.track_ids)
+      SPHG_CUDA(cudaMemcpyAsync(ids, s->idsA, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < n; ++i) vel[i] = make_float2(velp[i].x, velp[i].y);
+    if (!s->opt.track_ids)
+      for (int64_t i = 0; i < n; ++i) ids[i] = -1;
+  }
+  *bytes = need;
+  return SPHG_OK;
+}
+
+sphg_status sphg_restore(sphg_sim* s, const void* buf, uint64_t bytes, void* stream) {
+  if (!s || !buf || bytes < sizeof(SnapHeader)) return fail(SPHG_INVALID_ARG, "null or short snapshot");
+  SnapHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (h.magic != kSnapMagic || h.version != 1u) return fail(SPHG_INVALID_ARG, "not an sphg snapshot");
+  if (h.n != s->n || h.ninst != s->ninst || (int)h.precision != s->opt.precision)
+    return fail(SPHG_INVALID_ARG, "snapshot of a different handle shape or precision");
+  const int64_t n = s->n;
+  if (bytes < sizeof(SnapHeader) + (uint64_t)n * (sizeof(float2) * 2 + sizeof(uint32_t) + sizeof(int32_t)))
+    return fail(SPHG_INVALID_ARG, "truncated snapshot");
+  cudaStream_t st = (cudaStream_t)stream;
+  const char* p = static_cast<const char*>(buf) + sizeof(SnapHeader);
+  const float2* pos = reinterpret_cast<const float2*>(p);
+  const float2* vel = pos + n;
+  const uint32_t* key = reinterpret_cast<const uint32_t*>(vel + n);
+  const int32_t* ids = reinterpret_cast<const int32_t*>(key + n);
+  if (n > 0) {
+    // the saved (sorted) state becomes the uploaded state; split offsets stay
+    // relative to the saved cells (keyA), exactly as after an upload
+    SPHG_CUDA(cudaMemcpyAsync(s->posB, pos, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    SPHG_CUDA(cudaMemcpyAsync(s->velB, vel, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    SPHG_CUDA(cudaMemcpyAsync(s->keyA, key, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    if (s->opt.track_ids) SPHG_CUDA(cudaMemcpyAsync(s->idsB, ids, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    SPHG_CUDA(cudaMemsetAsync(s->scratch, 0, sizeof(uint32_t) * 4 * 256, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+  }
+  s->uploaded = true;
+  s->preloop_done = false;
+  return SPHG_OK;
+}
+
 sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
   if (!s || !ms || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state or null output");
   cudaStream_t st = (cudaStream_t)stream;

@@ -78,6 +78,10 @@ def lib():
         L.sphg_profile_step.restype = ctypes.c_int
         L.sphg_launches_per_step.argtypes = [SP]
         L.sphg_launches_per_step.restype = ctypes.c_int32
+        L.sphg_snapshot.argtypes = [SP, _vp, ctypes.POINTER(ctypes.c_uint64), _vp]
+        L.sphg_restore.argtypes = [SP, _vp, ctypes.c_uint64, _vp]
+        L.sphg_snapshot.restype = ctypes.c_int
+        L.sphg_restore.restype = ctypes.c_int
         L.sphg_server_create.argtypes = [ctypes.c_double, ctypes.c_int32, OP, ctypes.POINTER(SP)]
         L.sphg_server_destroy.argtypes = [SP]
         L.sphg_server_submit.argtypes = [SP, PP, ctypes.c_int64, _dp, _dp, _dp, _dp, ctypes.c_int64, _lp]
@@ -215,6 +219,18 @@ class Sim:
         check(lib().sphg_neighbor_lists(self._h, _ptr(offs, _lp), _ptr(idx, _ip),
                                         ctypes.byref(total), _stream(stream)))
         return offs, idx[:total.value]
+
+    def snapshot(self, stream=None):
+        """bytes of an exact-resume snapshot of the current state."""
+        size = ctypes.c_uint64(0)
+        check(lib().sphg_snapshot(self._h, None, ctypes.byref(size), _stream(stream)))
+        buf = ctypes.create_string_buffer(size.value)
+        check(lib().sphg_snapshot(self._h, buf, ctypes.byref(size), _stream(stream)))
+        return buf.raw
+
+    def restore(self, blob, stream=None):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        check(lib().sphg_restore(self._h, buf, len(blob), _stream(stream)))
 
     def profile_step(self, stream=None):
         """Milliseconds of keys, sort, reorder, density, force+integrate for one iteration."""
