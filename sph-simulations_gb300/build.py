@@ -1,4 +1,5 @@
-"""Builds libsphg.so (the CUDA library behind include/sphg.h) for sm_103a.
+"""Builds libsphg.so (the CUDA library behind include/sphg.h) for sm_103a, and
+the host driver sph_gb300_app (app/sph_gb300_app.cpp) linked against it.
 
 Each .cu translation unit is compiled in parallel with nvcc, then linked into
 one shared library next to this file.  Objects go to ``_build/``.
@@ -16,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsphg.so")
 HOST_APP = os.path.join(HERE, "sph_gb300_app")
+APP_SRC = os.path.join(HERE, "app", "sph_gb300_app.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + os.path.join(ROOT, "include")]
@@ -65,8 +67,15 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link of libsphg.so failed:\n%s%s" % (r.stdout, r.stderr))
+    if force or _stale(HOST_APP, [APP_SRC, LIB, os.path.join(ROOT, "include", "sphg.h")]):
+        gxx = shutil.which("g++") or "g++"
+        cmd = [gxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), APP_SRC, "-o", HOST_APP,
+               "-L" + HERE, "-lsphg", "-Wl,-rpath,$ORIGIN", "-pthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build of sph_gb300_app failed:\n%s%s" % (r.stdout, r.stderr))
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", HOST_APP)
     return LIB
 
 
