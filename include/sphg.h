@@ -58,6 +58,16 @@ typedef enum sphg_status {
 
 enum { SPHG_ORDER_MORTON = 0, SPHG_ORDER_ROWMAJOR = 1 };
 enum { SPHG_PRECISION_PLAIN = 0, SPHG_PRECISION_SPLIT = 1 };
+/* compute_type of the reference driver (app/simulation_configuration.h:479-537):
+ * SORTED  = `sorted`: the density pass walks the 3x3 cell stencil of the sorted
+ *           state (GenericForceComputation, core/compute/GenericForceComputation.tpp:35-253)
+ *           and hands the neighbours it accepts to the force pass;
+ * LISTS   = `lists` / `mp-lists`: every iteration assembles CSR neighbour lists
+ *           (count, scan, fill; MultipassNeighborLists,
+ *           core/algorithmic/MultipassNeighborLists.h:47-181) and the density
+ *           and force passes sum over them in list order
+ *           (MPListsForceComputation, core/compute/MPListsForceComputation.cpp:3-147). */
+enum { SPHG_COMPUTE_SORTED = 0, SPHG_COMPUTE_LISTS = 1 };
 
 /* Physics and domain of one instance.  sphg_default_params() fills the
  * reference's values: core/ConfigVariables.hpp:9-15 (H=1, TOL=1e-12,
@@ -92,6 +102,8 @@ typedef struct sphg_options {
   int32_t tile_bits;   /* density/force cell tiles of 2^b x 2^b cells staged in shared memory:
                           0 = default (off), 3..5 = that b (every instance in Morton order),
                           -1 = off (one thread per particle, L1-cached global loads) */
+  int32_t compute;     /* SPHG_COMPUTE_*; LISTS reads each iteration's list total back
+                          to size the lists, so it runs without CUDA graphs or cell tiles */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;
@@ -138,6 +150,19 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
  * total in *total; offs has n+1 entries. */
 sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_t* total,
                                 void* stream);
+
+/* The same lists with each list sorted ascending and delta-coded as
+ * Codifier::Encode does (core/encoders/Encoder.h:27-44: the first index, then
+ * idx[k] - idx[k-1] - 1).  The reference never calls its encoder on the active
+ * path (core/alg/GenericNeighborLists.tpp:75-78). */
+sphg_status sphg_neighbor_lists_encoded(sphg_sim* s, int64_t* offs, int32_t* enc, int64_t* total,
+                                        void* stream);
+/* Stand-alone delta codec of n CSR lists on DEVICE buffers (offs[n+1]);
+ * encode needs ascending lists; decode inverts it. */
+sphg_status sphg_delta_encode(const int64_t* offs, const int32_t* idx, int64_t n, int32_t* enc,
+                              void* stream);
+sphg_status sphg_delta_decode(const int64_t* offs, const int32_t* enc, int64_t n, int32_t* idx,
+                              void* stream);
 
 /* Binary snapshot of the current state in the device representation (positions
  * or split cell + offset, velocities, cell keys, creation indices) so a run can

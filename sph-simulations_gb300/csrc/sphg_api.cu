@@ -187,7 +187,27 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false) {
   if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
-  if (s->tile_bits) {
+  if (s->opt.compute == SPHG_COMPUTE_LISTS) {
+    // AssembleNeighborList: count, offsets, fill -- then density and forces over the lists
+    SPHG_CUDA(sphg::launch_lists_count_scan(a, prec, s->csr_counts, s->csr_offs, s->csr_sums, st));
+    SPHG_CUDA(cudaMemcpyAsync(&s->csr_total, s->csr_sums + sphg::lists_scan_tiles(s->n), sizeof(int64_t),
+                              cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+    if (s->csr_total > s->csr_cap) {
+      const int64_t cap = s->csr_total + s->csr_total / 4 + 1024;
+      if (s->csr_idx) SPHG_CUDA(cudaFree(s->csr_idx));
+      s->csr_idx = nullptr;
+      s->csr_cap = 0;
+      cudaError_t e = cudaMalloc(&s->csr_idx, (size_t)cap * sizeof(uint32_t));
+      if (e != cudaSuccess)
+        return fail(SPHG_OOM, std::string("neighbour-list buffer: ") + cudaGetErrorString(e));
+      s->csr_cap = cap;
+    }
+    const StepArgs b = s->args();
+    SPHG_CUDA(sphg::launch_lists_fill_packed(b, prec, s->csr_offs, s->csr_idx, s->csr_cap, st));
+    SPHG_CUDA(sphg::launch_density(b, prec, st, true));
+    SPHG_CUDA(sphg::launch_force(b, prec, sphg::kForceIntegrate, st, true));
+  } else if (s->tile_bits) {
     SPHG_CUDA(sphg::launch_tiled(a, prec, false, st));
     SPHG_CUDA(sphg::launch_tiled(a, prec, true, st));
   } else {
@@ -241,6 +261,13 @@ sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p) {
   if (tb == 0) tb = -1;  // default: one thread per particle (faster than the tiles at these densities)
   if (tb > 0 && (!all_morton || tb < 3 || tb > 5))
     return fail(SPHG_INVALID_ARG, "cell tiles need Morton order on every instance and tile_bits in 3..5");
+  if (s->opt.compute != SPHG_COMPUTE_SORTED && s->opt.compute != SPHG_COMPUTE_LISTS)
+    return fail(SPHG_INVALID_ARG, "unknown compute mode");
+  if (s->opt.compute == SPHG_COMPUTE_LISTS) {
+    if (tb > 0) return fail(SPHG_INVALID_ARG, "the lists compute mode runs without cell tiles");
+    tb = -1;
+    s->opt.use_graph = 0;  // every iteration reads its list total back
+  }
   s->tile_bits = tb > 0 ? tb : 0;
   return SPHG_OK;
 }
@@ -280,7 +307,7 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
   s->diag_chunks = diag_chunks;
   // per-particle neighbour slots filled by the density pass and read by the
   // force pass (indices are packed as j << 5, so only below 2^27 particles)
-  s->nbr_slots = (N < ((size_t)1 << 27)) ? 12 : 0;
+  s->nbr_slots = (N < ((size_t)1 << 27) && s->opt.compute == SPHG_COMPUTE_SORTED) ? 12 : 0;
   auto layout = [&](Arena& A) {
     s->ddesc = A.take<InstDesc>(ninst);
     s->dbegins = A.take<int32_t>(ninst);
@@ -306,6 +333,11 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     if (s->nbr_slots) {
       s->nbr = A.take<uint32_t>(N * (size_t)s->nbr_slots);
       s->ncount = A.take<uint32_t>(N);
+    }
+    if (s->opt.compute == SPHG_COMPUTE_LISTS) {
+      s->csr_counts = A.take<int32_t>(N);
+      s->csr_offs = A.take<int64_t>(N + 1);
+      s->csr_sums = A.take<int64_t>((size_t)sphg::lists_scan_tiles((int64_t)N) + 1);
     }
     if (s->tile_bits) {
       s->tile_ranges = A.take<uint2>((keys >> (2 * s->tile_bits)) + 1);
@@ -369,6 +401,7 @@ sphg_status destroy_impl(sphg_sim* s) {
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   if (s->arena.base) cudaFree(s->arena.base);
+  if (s->csr_idx) cudaFree(s->csr_idx);
   delete s;
   return SPHG_OK;
 }
@@ -406,6 +439,7 @@ void sphg_default_options(sphg_options* o) {
   o->track_ids = 1;
   o->use_graph = 1;
   o->tile_bits = 0;
+  o->compute = SPHG_COMPUTE_SORTED;
 }
 
 const char* sphg_last_error_string(void) { return g_err.c_str(); }
@@ -640,6 +674,29 @@ sphg_status sphg_neighbor_lists(sphg_sim* s, int64_t* offs, int32_t* idx, int64_
   return SPHG_OK;
 }
 
+sphg_status sphg_neighbor_lists_encoded(sphg_sim* s, int64_t* offs, int32_t* enc, int64_t* total,
+                                        void* stream) {
+  if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
+  std::string err;
+  int st = sphg::lists_impl(s->args(), s->opt.precision, offs, enc, total, (cudaStream_t)stream, &err, true);
+  if (st != SPHG_OK) return fail((sphg_status)st, err);
+  return SPHG_OK;
+}
+
+sphg_status sphg_delta_encode(const int64_t* offs, const int32_t* idx, int64_t n, int32_t* enc,
+                              void* stream) {
+  if (n < 0 || (n > 0 && (!offs || !idx || !enc))) return fail(SPHG_INVALID_ARG, "null buffer or n < 0");
+  SPHG_CUDA(sphg::launch_delta(true, offs, idx, n, enc, (cudaStream_t)stream));
+  return SPHG_OK;
+}
+
+sphg_status sphg_delta_decode(const int64_t* offs, const int32_t* enc, int64_t n, int32_t* idx,
+                              void* stream) {
+  if (n < 0 || (n > 0 && (!offs || !idx || !enc))) return fail(SPHG_INVALID_ARG, "null buffer or n < 0");
+  SPHG_CUDA(sphg::launch_delta(false, offs, enc, n, idx, (cudaStream_t)stream));
+  return SPHG_OK;
+}
+
 namespace {
 struct SnapHeader {
   uint64_t magic;       // "SPHGSNAP"
@@ -752,8 +809,9 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
 int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
-  // radix passes + reorder + density + force (+ the sort's histogram kernel with tiles)
-  return passes + 3 + (s->tile_bits ? 1 : 0);
+  // the sort's histogram kernel + radix passes + reorder + density + force
+  // (+ list count, three scan kernels and list fill in the lists mode)
+  return passes + 4 + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
 }
 
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

@@ -57,6 +57,11 @@ struct sphg_sim {
   uint32_t* tile_list = nullptr;
   uint32_t *nbr = nullptr, *ncount = nullptr;
   int nbr_slots = 0;
+  // lists mode: CSR of each iteration; the index buffer grows with the list total
+  int32_t* csr_counts = nullptr;
+  int64_t *csr_offs = nullptr, *csr_sums = nullptr;
+  uint32_t* csr_idx = nullptr;
+  int64_t csr_cap = 0, csr_total = 0;
   size_t cap_n = 0;             // arena capacity (particles)
   uint64_t cap_keys = 0;        // arena capacity (cell keys)
   int cap_inst = 0;             // arena capacity (instances)
@@ -102,6 +107,8 @@ struct sphg_sim {
     a.key_passes = (key_bits + 7) / 8;
     a.ncount = ncount;
     a.nbr_slots = nbr_slots;
+    a.csr_offs = csr_offs;
+    a.csr_idx = csr_idx;
     return a;
   }
 };

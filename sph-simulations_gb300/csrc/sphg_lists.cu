@@ -48,6 +48,24 @@ __global__ void __launch_bounds__(kListThreads) lists_fill(StepArgs a, const int
                                 [&](uint32_t j, float, float, float, uint32_t) { idx[o++] = (int32_t)j; });
 }
 
+// Lists mode: the same walk, entries packed as j << 5 | tag (stencil offset and
+// periodic-wrap bit, read back by the density and force passes); at most cap
+// entries are written (the host sized the buffer from this iteration's total).
+template <int PREC, bool BATCHED>
+__global__ void __launch_bounds__(kListThreads) lists_fill_packed(StepArgs a, const int64_t* offs,
+                                                                  uint32_t* idx, int64_t cap) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const InstDesc d = inst_of<BATCHED>(a, i);
+  int64_t o = offs[i];
+  int cx, cy;
+  for_each_neighbor<PREC, true>(a, d, a.keyA[i], a.posA[i], cx, cy,
+                                [&](uint32_t j, float, float, float, uint32_t tag) {
+                                  if (o < cap) idx[o] = (j << 5) | tag;
+                                  ++o;
+                                });
+}
+
 // Exclusive scan of int32 counts into int64 offsets (offs[n] = total).
 __device__ __forceinline__ int64_t block_excl_scan(int64_t v, int64_t* warp_tot, int64_t& total) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -118,12 +136,104 @@ __global__ void scan_add(int64_t* offs, int64_t n, const int64_t* tile_sums,
   if (i == n) offs[n] = *total;
 }
 
+// Delta codec of CSR lists (Codifier::Encode, core/encoders/Encoder.h:27-44):
+// the first index of a list verbatim, then idx[k] - idx[k-1] - 1, which needs
+// each list ascending.  One thread per list.
+__global__ void lists_sort_ascending(const int64_t* offs, int32_t* idx, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b = offs[i], e = offs[i + 1];
+  for (int64_t q = b + 1; q < e; ++q) {  // insertion sort: lists hold a few dozen entries
+    const int32_t v = idx[q];
+    int64_t r = q - 1;
+    while (r >= b && idx[r] > v) {
+      idx[r + 1] = idx[r];
+      --r;
+    }
+    idx[r + 1] = v;
+  }
+}
+
+__global__ void delta_encode_kernel(const int64_t* offs, const int32_t* idx, int64_t n, int32_t* enc) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b = offs[i], e = offs[i + 1];
+  if (b >= e) return;
+  int32_t prev = idx[b];
+  enc[b] = prev;
+  for (int64_t q = b + 1; q < e; ++q) {
+    const int32_t v = idx[q];
+    enc[q] = v - prev - 1;
+    prev = v;
+  }
+}
+
+__global__ void delta_decode_kernel(const int64_t* offs, const int32_t* enc, int64_t n, int32_t* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b = offs[i], e = offs[i + 1];
+  if (b >= e) return;
+  int32_t v = enc[b];
+  out[b] = v;
+  for (int64_t q = b + 1; q < e; ++q) {
+    v = v + enc[q] + 1;
+    out[q] = v;
+  }
+}
+
+cudaError_t launch_delta(bool encode, const int64_t* offs, const int32_t* in, int64_t n, int32_t* out,
+                         cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  if (encode) delta_encode_kernel<<<g, 256, 0, st>>>(offs, in, n, out);
+  else delta_decode_kernel<<<g, 256, 0, st>>>(offs, in, n, out);
+  return cudaGetLastError();
+}
+
+int lists_scan_tiles(int64_t n) { return (int)((n + kScanTile - 1) / kScanTile); }
+
+cudaError_t launch_lists_count_scan(const StepArgs& a, int precision, int32_t* counts, int64_t* offs,
+                                    int64_t* sums, cudaStream_t st) {
+  const int64_t n = a.n;
+  if (n == 0) return cudaSuccess;
+  const int ntiles = lists_scan_tiles(n);
+  const unsigned g = (unsigned)((n + kListThreads - 1) / kListThreads);
+  const bool batched = (a.ninst > 1 || a.force_batched);
+  if (precision) {
+    if (batched) lists_count<1, true><<<g, kListThreads, 0, st>>>(a, counts);
+    else lists_count<1, false><<<g, kListThreads, 0, st>>>(a, counts);
+  } else {
+    if (batched) lists_count<0, true><<<g, kListThreads, 0, st>>>(a, counts);
+    else lists_count<0, false><<<g, kListThreads, 0, st>>>(a, counts);
+  }
+  scan_tiles<<<ntiles, kScanThreads, 0, st>>>(counts, n, offs, sums);
+  scan_tile_sums<<<1, kScanThreads, 0, st>>>(sums, ntiles, sums + ntiles);
+  scan_add<<<(unsigned)((n + 1 + 255) / 256), 256, 0, st>>>(offs, n, sums, sums + ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int64_t* offs,
+                                     uint32_t* idx, int64_t cap, cudaStream_t st) {
+  const int64_t n = a.n;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = (unsigned)((n + kListThreads - 1) / kListThreads);
+  const bool batched = (a.ninst > 1 || a.force_batched);
+  if (precision) {
+    if (batched) lists_fill_packed<1, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+    else lists_fill_packed<1, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+  } else {
+    if (batched) lists_fill_packed<0, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+    else lists_fill_packed<0, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace sphg
 
 namespace sphg {
 
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
-               cudaStream_t st, std::string* err) {
+               cudaStream_t st, std::string* err, bool encoded) {
   const int64_t n = a.n;
   if (total) *total = 0;
   if (n == 0) {
@@ -182,8 +292,19 @@ int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, in
       if (batched) lists_fill<0, true><<<g, kListThreads, 0, st>>>(a, doffs, didx);
       else lists_fill<0, false><<<g, kListThreads, 0, st>>>(a, doffs, didx);
     }
-    ok = ck(cudaGetLastError(), "list fill launch") &&
-         ck(cudaMemcpyAsync(idx, didx, tot * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "copy");
+    if (encoded) {  // ascending lists, delta-coded in place of the counts buffer
+      int32_t* denc = nullptr;
+      ok = ck(cudaMallocAsync((void**)&denc, tot * sizeof(int32_t), st), "cudaMallocAsync");
+      if (!ok) { cleanup(); return SPHG_OOM; }
+      lists_sort_ascending<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(doffs, didx, n);
+      ok = ck(launch_delta(true, doffs, didx, n, denc, st), "delta encode launch") &&
+           ck(cudaMemcpyAsync(idx, denc, tot * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "copy");
+      cudaFreeAsync(denc, st);
+      if (!ok) { cleanup(); return SPHG_CUDA_ERROR; }
+    } else {
+      ok = ck(cudaGetLastError(), "list fill launch") &&
+           ck(cudaMemcpyAsync(idx, didx, tot * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "copy");
+    }
     if (!ok) { cleanup(); return SPHG_CUDA_ERROR; }
   }
   cleanup();

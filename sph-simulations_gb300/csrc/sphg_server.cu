@@ -291,6 +291,7 @@ sphg_status sphg_server_create(double hbm_budget_bytes, int32_t max_instances, c
   sim->opt.tile_bits = -1;   // layouts change every few ticks: per-particle kernels
   sim->opt.use_graph = 0;    // ... and direct launches
   sim->force_batched = 1;    // same kernels (and bits) whatever the batch size
+  sim->opt.compute = SPHG_COMPUTE_SORTED;
   sphg_status st = check_options(sim, 0, nullptr);
   if (st != SPHG_OK) {
     delete sim;

@@ -104,7 +104,25 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- density + pressure
-template <int PREC, bool BATCHED>
+// Pair vector x_i - x_j of a recorded neighbour entry (j << 5 | tag): the tag's
+// stencil offset k = 3 (c1 + 1) + (c2 + 1) moves the split offsets into one
+// cell frame; bit 4 marks a periodic wrap (plain positions: minimum image).
+template <int PREC>
+__device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 pj, uint32_t e,
+                                          float& dx, float& dy) {
+  if (PREC == 0 && (e & 16u)) {
+    wrapped_pair(d, pi, pj, dx, dy);
+  } else {
+    const uint32_t k = e & 15u;
+    const int c1 = (int)(k / 3) - 1, c2 = (int)(k % 3) - 1;
+    const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
+    const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
+    dx = (pi.x - pj.x) - shx;
+    dy = (pi.y - pj.y) - shy;
+  }
+}
+
+template <int PREC, bool BATCHED, bool CSR>
 __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -114,19 +132,32 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   typename std::conditional<PREC == 1, CSum, PSum>::type S;
   int cx, cy;
   const float inv_h2 = d.inv_h2;
-  uint32_t* __restrict__ nbr = a.nbr;
-  const uint32_t slots = (uint32_t)a.nbr_slots;
-  const size_t n = (size_t)a.n;
-  uint32_t cnt = 0;
-  for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
-    float t = fmaf(-r2, inv_h2, 1.0f);
-    S.add(t * t * t);
-    if (nbr && j != (uint32_t)i) {  // record the pair for the force pass
-      if (cnt < slots) nbr[cnt * n + i] = (j << 5) | tag;
-      ++cnt;
+  if constexpr (CSR) {
+    // MPListsForceComputation::ApproximateDensity: the list in its order, self included
+    const int64_t b = a.csr_offs[i], e = a.csr_offs[i + 1];
+    for (int64_t q = b; q < e; ++q) {
+      const uint32_t ent = __ldg(a.csr_idx + q);
+      float dx, dy;
+      entry_vec<PREC>(d, pi, __ldg(a.posA + (ent >> 5)), ent, dx, dy);
+      const float r2 = fmaf(dx, dx, dy * dy);
+      const float t = fmaf(-r2, inv_h2, 1.0f);
+      S.add(t * t * t);
     }
-  });
-  if (nbr) a.ncount[i] = cnt;
+  } else {
+    uint32_t* __restrict__ nbr = a.nbr;
+    const uint32_t slots = (uint32_t)a.nbr_slots;
+    const size_t n = (size_t)a.n;
+    uint32_t cnt = 0;
+    for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
+      float t = fmaf(-r2, inv_h2, 1.0f);
+      S.add(t * t * t);
+      if (nbr && j != (uint32_t)i) {  // record the pair for the force pass
+        if (cnt < slots) nbr[cnt * n + i] = (j << 5) | tag;
+        ++cnt;
+      }
+    });
+    if (nbr) a.ncount[i] = cnt;
+  }
   float rho, drho;
   if constexpr (PREC == 1) {
     rho = d.wd * S.value();
@@ -149,11 +180,11 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 // kForceBuf neighbours handles the extra ones inline during the scan.
 constexpr int kForceBuf = 12;
 
-template <int PREC, bool BATCHED, int MODE>
+template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
                                               uint32_t (*bj)[kThreads]);
 
-template <int PREC, bool BATCHED, int MODE>
+template <int PREC, bool BATCHED, int MODE, bool CSR>
 __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   __shared__ float2 bd[kForceBuf][kThreads];
   __shared__ uint32_t bj[kForceBuf][kThreads];
@@ -166,13 +197,13 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   uint32_t key = 0;
-  if (valid) key = force_one<PREC, BATCHED, MODE>(a, i, bd, bj);
+  if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, bd, bj);
   if (hist) histogram_keys(a, hs, valid, key);
 }
 
 // Forces on particle i; in integrate mode also the update and the new key
 // (returned), in force-only mode the acceleration is stored.
-template <int PREC, bool BATCHED, int MODE>
+template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
                                               uint32_t (*bj)[kThreads]) {
   const InstDesc d = inst_of<BATCHED>(a, i);
@@ -211,26 +242,29 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
     }
   };
   int cx, cy;
-  const uint32_t cnt = a.nbr ? a.ncount[i] : 0xffffffffu;
-  if (cnt <= (uint32_t)a.nbr_slots) {
+  const uint32_t cnt = CSR ? 0u : (a.nbr ? a.ncount[i] : 0xffffffffu);
+  if (CSR) {
+    // MPListsForceComputation::ComputeForces: the list in its order (self skipped:
+    // its pressure term is excluded by r > TOL and its viscosity term is zero)
+    decode_code(d, key - d.cell_base, cx, cy);
+    const int64_t b = a.csr_offs[i], e = a.csr_offs[i + 1];
+    for (int64_t q = b; q < e; ++q) {
+      const uint32_t ent = __ldg(a.csr_idx + q);
+      const uint32_t j = ent >> 5;
+      if (j == (uint32_t)i) continue;
+      float dx, dy;
+      entry_vec<PREC>(d, pi, __ldg(a.posA + j), ent, dx, dy);
+      pair(j, dx, dy);
+    }
+  } else if (cnt <= (uint32_t)a.nbr_slots) {
     // the density pass recorded this particle's neighbours (stencil order)
     decode_code(d, key - d.cell_base, cx, cy);
     const size_t n = (size_t)a.n;
     for (uint32_t q = 0; q < cnt; ++q) {
       const uint32_t e = __ldg(a.nbr + q * n + i);
-      const uint32_t j = e >> 5, k = e & 15u;
-      const float2 pj = __ldg(a.posA + j);
       float dx, dy;
-      if (PREC == 0 && (e & 16u)) {
-        wrapped_pair(d, pi, pj, dx, dy);
-      } else {
-        const int c1 = (int)(k / 3) - 1, c2 = (int)(k % 3) - 1;
-        const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
-        const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
-        dx = (pi.x - pj.x) - shx;
-        dy = (pi.y - pj.y) - shy;
-      }
-      pair(j, dx, dy);
+      entry_vec<PREC>(d, pi, __ldg(a.posA + (e >> 5)), e, dx, dy);
+      pair(e >> 5, dx, dy);
     }
   } else {
     int nb = 0;
@@ -380,18 +414,26 @@ cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s) {
+cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s, bool csr) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
-  SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_density);
+  const bool b = (a.ninst > 1 || a.force_batched);
+  if (csr) SPHG_DISPATCH2(precision, b, step_density, , true);
+  else SPHG_DISPATCH2(precision, b, step_density, , false);
   return cudaGetLastError();
 }
 
-cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s) {
+cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s, bool csr) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
-  if (mode == kForceOnly) SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_force, , kForceOnly);
-  else SPHG_DISPATCH2(precision, (a.ninst > 1 || a.force_batched), step_force, , kForceIntegrate);
+  const bool b = (a.ninst > 1 || a.force_batched);
+  if (csr) {
+    if (mode == kForceOnly) SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, true);
+    else SPHG_DISPATCH2(precision, b, step_force, , kForceIntegrate, true);
+  } else {
+    if (mode == kForceOnly) SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, false);
+    else SPHG_DISPATCH2(precision, b, step_force, , kForceIntegrate, false);
+  }
   return cudaGetLastError();
 }
 

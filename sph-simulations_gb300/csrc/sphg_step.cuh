@@ -35,6 +35,8 @@ struct StepArgs {
   uint32_t* nbr;               // [nbr_slots][n] neighbours found by the density pass: j << 5 | tag
   uint32_t* ncount;            // [n] neighbours of each particle (> nbr_slots: list overflowed)
   int nbr_slots;
+  const int64_t* csr_offs;     // [n+1] CSR neighbour lists of this iteration (lists mode)
+  const uint32_t* csr_idx;     // j << 5 | tag entries, self included, list order
   uint32_t* ghist;             // digit histograms of the next sort (accumulated by the key writers)
   int key_passes;              // radix passes of the next sort
   uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
@@ -51,8 +53,15 @@ enum ForceMode { kForceIntegrate = 0, kForceOnly = 1 };
 
 cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s);
 cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s);
-cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s);
+cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s, bool csr = false);
+cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s, bool csr = false);
+// Lists mode: per-particle counts, exclusive scan to int64 offsets (the total
+// lands in sums[scan_tiles(n)]), fill of packed entries (at most cap).
+int lists_scan_tiles(int64_t n);
+cudaError_t launch_lists_count_scan(const StepArgs& a, int precision, int32_t* counts, int64_t* offs,
+                                    int64_t* sums, cudaStream_t st);
+cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int64_t* offs,
+                                     uint32_t* idx, int64_t cap, cudaStream_t st);
 // Per-instance diagnostics: partial sums per (chunk, instance) then a fixed-order
 // final sum; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx, sum m vy, nonfinite.
 cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
@@ -60,7 +69,10 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
 int diag_chunks(int64_t max_inst_n);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
-               cudaStream_t st, std::string* err);
+               cudaStream_t st, std::string* err, bool encoded = false);
+// Delta codec of CSR lists on device buffers (encode: in = ascending lists).
+cudaError_t launch_delta(bool encode, const int64_t* offs, const int32_t* in, int64_t n, int32_t* out,
+                         cudaStream_t st);
 // Cell-tile density (force == false) or force + integration + next keys (force == true).
 cudaError_t launch_tiled(const StepArgs& a, int precision, bool force, cudaStream_t s);
 size_t tile_smem_bytes(int tb, int cap, bool force);

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libsphg.so")
 OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY, NOT_READY = range(8)
 ORDER = {"morton": 0, "rowmajor": 1}
 PLAIN, SPLIT = 0, 1
+SORTED, LISTS = 0, 1
 DBG_KEYS, DBG_PERM, DBG_UNSORTED_KEYS, DBG_POS_NEXT, DBG_VEL_NEXT = range(5)
 
 
@@ -39,7 +40,8 @@ class Params(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32)]
+                ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
+                ("compute", ctypes.c_int32)]
 
 
 _lib = None
@@ -93,6 +95,11 @@ def lib():
             getattr(L, f).restype = ctypes.c_int
         L.sphg_sort_pairs.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp]
         L.sphg_cell_keys.argtypes = [PP, _vp, _vp, ctypes.c_int64, _vp, _vp]
+        L.sphg_neighbor_lists_encoded.argtypes = [SP, _lp, _ip, _lp, _vp]
+        L.sphg_delta_encode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
+        L.sphg_delta_decode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
+        for f in ("sphg_neighbor_lists_encoded", "sphg_delta_encode", "sphg_delta_decode"):
+            getattr(L, f).restype = ctypes.c_int
         for f in ("sphg_create", "sphg_create_batch", "sphg_destroy", "sphg_upload",
                   "sphg_preloop", "sphg_step", "sphg_download", "sphg_diagnostics",
                   "sphg_get_debug", "sphg_neighbor_lists", "sphg_sort_pairs", "sphg_cell_keys"):
@@ -120,13 +127,15 @@ def params(**kw):
     return p
 
 
-def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0):
+def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None):
     o = Options()
     lib().sphg_default_options(ctypes.byref(o))
     o.precision = precision
     o.track_ids = track_ids
     o.use_graph = use_graph
     o.tile_bits = tile_bits
+    if compute is not None:
+        o.compute = {"sorted": SORTED, "lists": LISTS, "mp-lists": LISTS}.get(compute, compute)
     return o
 
 
@@ -219,6 +228,17 @@ class Sim:
         check(lib().sphg_neighbor_lists(self._h, _ptr(offs, _lp), _ptr(idx, _ip),
                                         ctypes.byref(total), _stream(stream)))
         return offs, idx[:total.value]
+
+    def neighbor_lists_encoded(self, stream=None):
+        """Ascending lists, delta-coded (Codifier::Encode)."""
+        total = ctypes.c_int64(0)
+        offs = np.empty(self.n + 1, np.int64)
+        check(lib().sphg_neighbor_lists_encoded(self._h, _ptr(offs, _lp), None, ctypes.byref(total),
+                                                _stream(stream)))
+        enc = np.empty(max(total.value, 1), np.int32)
+        check(lib().sphg_neighbor_lists_encoded(self._h, _ptr(offs, _lp), _ptr(enc, _ip),
+                                                ctypes.byref(total), _stream(stream)))
+        return offs, enc[:total.value]
 
     def snapshot(self, stream=None):
         """bytes of an exact-resume snapshot of the current state."""
@@ -317,6 +337,15 @@ def sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, n, bits, st
     """Stand-alone radix sort on caller-owned device buffers (raw pointers)."""
     check(lib().sphg_sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, int(n),
                                 int(bits), _stream(stream)))
+
+
+def delta_encode(offs_ptr, idx_ptr, n, enc_ptr, stream=None):
+    """Delta codec of n CSR lists on caller-owned device buffers (raw pointers)."""
+    check(lib().sphg_delta_encode(offs_ptr, idx_ptr, int(n), enc_ptr, _stream(stream)))
+
+
+def delta_decode(offs_ptr, enc_ptr, n, idx_ptr, stream=None):
+    check(lib().sphg_delta_decode(offs_ptr, enc_ptr, int(n), idx_ptr, _stream(stream)))
 
 
 def cell_keys(prm, x_ptr, y_ptr, n, keys_ptr, stream=None):

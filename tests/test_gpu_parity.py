@@ -564,3 +564,115 @@ def test_snapshot_resume_is_exact(prec):
         c.restore(blob)
     for h in (a, b, c):
         h.close()
+
+
+# ---------------------------------------------------------------- lists compute mode + delta codec
+def test_lists_mode_matches_reference_lists_golden(golden):
+    """compute=lists on the fixture's sorted state: the reference's
+    MPListsForceComputation density and forces (FP64) within the FP32 tolerances."""
+    S = _sphg()
+    g = golden("lists")
+    n = len(g["x"])
+    prm = S.params(order="morton", h=float(g["h"]), dt=1e-5, lo=(0, 0), hi=(1, 1))
+    sim = S.Sim(prm, n, S.options(compute="lists"))
+    sim.upload(g["x"], g["y"], g["vx"], g["vy"])
+    sim.preloop()
+    out = sim.download()
+    ids = out["ids"]
+    assert rel_rho(out["rho"], g["mpl_rho"][ids]) <= RHO_TOL
+    assert rel_acc(out["fx"], out["fy"], g["mpl_fx"][ids], g["mpl_fy"][ids]) <= ACC_TOL
+    offs, idx = sim.neighbor_lists()
+    assert (offs == g["mpl_offs"]).all() and (idx == g["mpl_idx"]).all()
+    sim.close()
+
+
+@pytest.mark.parametrize("prec", ["plain", "split"])
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+def test_lists_mode_steps_match_oracle_and_sorted_mode(prec, order):
+    S = _sphg()
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    x, y, vx, vy = jittered(48, 40, 0.005, seed=21, vel=0.3)
+    kw = dict(order=order, h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.4, 0.3))
+    prm = S.params(**kw)
+    p = O.params(**kw)
+    lists = S.Sim(prm, len(x), S.options(precision=P, compute="lists"))
+    srt = S.Sim(prm, len(x), S.options(precision=P))
+    for s in (lists, srt):
+        s.upload(x, y, vx, vy)
+        s.preloop()
+    for k in (0, 7):
+        if k:
+            lists.step(k)
+            srt.step(k)
+        a = lists.download()
+        b = srt.download()
+        _, _, _, rho, fx, fy = oracle_state(p, a)
+        assert rel_rho(a["rho"], rho) <= RHO_TOL
+        assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+        oa, ob = np.argsort(a["ids"]), np.argsort(b["ids"])  # slot orders may differ at cell edges
+        for f in ("x", "y", "vx", "vy", "rho"):
+            np.testing.assert_allclose(a[f][oa], b[f][ob], rtol=1e-5, atol=1e-6 * np.abs(b[f]).max())
+    assert lists.launches_per_step() == srt.launches_per_step() + 5
+    lists.close()
+    srt.close()
+
+
+def test_lists_mode_periodic_and_batched():
+    """Lists mode over a batch holding a periodic Taylor-Green box and a walled box."""
+    import workloads as W
+    S = _sphg()
+    prm1, x1, y1, vx1, vy1, _ = W.taylor_green(24, seed=3)
+    rng = np.random.default_rng(4)
+    prm2, x2, y2 = W.dam_break_sized(700, 1.0, 0.005, rng, alpha=0.1)
+    prms = [S.params(**prm1), S.params(**prm2)]
+    counts = [len(x1), len(x2)]
+    cat = [np.concatenate(v) for v in ((x1, x2), (y1, y2), (vx1, np.zeros(len(x2))), (vy1, np.zeros(len(x2))))]
+    outs = []
+    for mode in ("lists", "sorted"):
+        sim = S.Sim(prms, counts, S.options(precision=S.SPLIT, compute=mode))
+        sim.upload(*cat)
+        sim.preloop()
+        sim.step(10)
+        outs.append(sim.download())
+        sim.close()
+    oa, ob = np.argsort(outs[0]["ids"]), np.argsort(outs[1]["ids"])
+    for f in ("x", "y", "vx", "vy", "rho"):
+        np.testing.assert_allclose(outs[0][f][oa], outs[1][f][ob], rtol=1e-5,
+                                   atol=1e-6 * np.abs(outs[1][f]).max())
+    # accelerations: the two summation orders differ by rounding, which the
+    # pressure k (rho - rho0) amplifies by rho / (rho - rho0)
+    assert rel_acc(outs[0]["fx"][oa], outs[0]["fy"][oa], outs[1]["fx"][ob], outs[1]["fy"][ob]) <= 1e-4
+
+
+def test_encoded_lists_round_trip(golden):
+    """GPU delta codec: encoded lists equal Codifier::Encode of the ascending lists,
+    the device decoder inverts the device encoder, and the reference's own
+    encoder output (fixture) is reproduced."""
+    import torch
+    S = _sphg()
+    x, y, vx, vy = jittered(30, 30, 0.005, seed=8)
+    prm = S.params(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.2, 0.2))
+    sim = S.Sim(prm, len(x))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    offs, idx = sim.neighbor_lists()
+    eoffs, enc = sim.neighbor_lists_encoded()
+    assert (eoffs == offs).all()
+    asc = idx.copy()
+    for i in range(len(offs) - 1):
+        asc[offs[i]:offs[i + 1]] = np.sort(idx[offs[i]:offs[i + 1]])
+    assert (enc == O.delta_encode(offs, asc)).all()
+    sim.close()
+    dev = torch.device("cuda:0")
+    for o_, a_, want in ((offs, asc, O.delta_encode(offs, asc)),
+                         (golden("lists")["enc_offs"], golden("lists")["enc_in"], golden("lists")["enc_out"])):
+        d_offs = torch.from_numpy(np.ascontiguousarray(o_, np.int64)).to(dev)
+        d_in = torch.from_numpy(np.ascontiguousarray(a_, np.int32)).to(dev)
+        d_enc = torch.empty_like(d_in)
+        d_dec = torch.empty_like(d_in)
+        n = len(o_) - 1
+        S.delta_encode(d_offs.data_ptr(), d_in.data_ptr(), n, d_enc.data_ptr())
+        S.delta_decode(d_offs.data_ptr(), d_enc.data_ptr(), n, d_dec.data_ptr())
+        torch.cuda.synchronize()
+        assert (d_enc.cpu().numpy() == want).all()
+        assert (d_dec.cpu().numpy() == a_).all()
