@@ -47,7 +47,9 @@ UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
 # DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
 # summed over one iteration's kernels); filled from the committed profile summaries
-TRAFFIC_PER_PARTICLE_STEP = {}
+# (profiles/traffic_dam_break_1m.md: 126.5 MB per iteration of 1,000,000 particles,
+# caches flushed before each captured launch)
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 126.5}
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -304,7 +306,10 @@ def run_gpu(args):
     hbm, src = peaks()
     achieved = value * BYTES_PER_PARTICLE_STEP / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": TRAFFIC_PER_PARTICLE_STEP.get(args.workload),
+                "frac": achieved / hbm,
+                "traffic": (TRAFFIC_PER_PARTICLE_STEP[args.workload] * n
+                            if args.workload in TRAFFIC_PER_PARTICLE_STEP else None),
+                "traffic_unit": "DRAM bytes per main-loop iteration (ncu)",
                 "peak_source": src,
                 "kernel": "one main-loop iteration (radix sort + reorder + density + force)",
                 "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP}

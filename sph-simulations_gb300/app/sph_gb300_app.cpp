@@ -1,6 +1,8 @@
 // Host driver for the GB300 path: the reference's driver loop (app/main.cpp:20-56
 // with app/simulation_configuration.h) selected by `compute_type=gb300`, running
 // the pre-loop and main loop through the C ABI of include/sphg.h.
+// compute_type=sorted is an alias of gb300; lists and mp-lists select the
+// library's lists compute mode (CSR lists assembled every iteration).
 //
 // Unchanged from the reference, so an existing run directory works as is:
 //   * the configuration file and its keys (config/example.txt; parser semantics
@@ -310,9 +312,10 @@ int main(int argc, char** argv) {
     std::cerr << "[Error] order must be morton or rowmajor, got '" << order << "'" << std::endl;
     return 1;
   }
-  if (ctype != "gb300" && ctype != "sorted") {
-    std::cerr << "[Error] compute_type '" << ctype << "' is not served by this driver (gb300 or sorted)"
-              << std::endl;
+  const bool lists = ctype == "lists" || ctype == "mp-lists";
+  if (ctype != "gb300" && ctype != "sorted" && !lists) {
+    std::cerr << "[Error] compute_type '" << ctype
+              << "' is not served by this driver (gb300, sorted, lists or mp-lists)" << std::endl;
     return 1;
   }
 
@@ -338,13 +341,15 @@ int main(int argc, char** argv) {
   sphg_default_options(&o);
   o.precision = cfg.str("precision", "plain") == "split" ? SPHG_PRECISION_SPLIT : SPHG_PRECISION_PLAIN;
   o.use_graph = (int32_t)cfg.integer("use_graph", 1);
+  o.compute = lists ? SPHG_COMPUTE_LISTS : SPHG_COMPUTE_SORTED;
 
   std::cout << "[Configuration] Domain size: " << Lx << " " << Ly << " 0\n";
   std::cout << "[Configuration] Particles=" << N << "\n[Configuration] steps=" << steps
             << "\n[Configuration] dt=" << dt << "\n[Configuration] output frequency=" << ckpt_freq << "\n";
   std::cout << "[Configuration] H=" << p.h << " GAS_CONSTANT=" << p.k << " RHO_0=" << p.rho0 << " MU=" << p.mu
             << "\n";
-  std::cout << "[Configuration] Using " << order << " ordering, compute type gb300 ("
+  std::cout << "[Configuration] Using " << order << " ordering, compute type gb300/"
+            << (lists ? "lists" : "sorted") << " ("
             << (o.precision == SPHG_PRECISION_SPLIT ? "split" : "plain") << " precision)\n";
   std::cout << "[Configuration] Configuration complete." << std::endl;
   if (dry) return 0;

@@ -51,11 +51,11 @@ def _match(points, ref):
     return d
 
 
-@pytest.mark.parametrize("order", ["rowmajor", "morton"])
-def test_driver_matches_oracle_run(tmp_path, order):
+@pytest.mark.parametrize("order,ctype", [("rowmajor", "gb300"), ("morton", "sorted"), ("morton", "mp-lists")])
+def test_driver_matches_oracle_run(tmp_path, order, ctype):
     app = _app()
     cfg = str(tmp_path / "example.txt")
-    kv = _cfg(cfg, order=order, bool_measure_neighborhood=1)
+    kv = _cfg(cfg, order=order, compute_type=ctype, bool_measure_neighborhood=1)
     out = _run(app, cfg, str(tmp_path))
     heads = _headers(out)
     assert sorted(heads) == list(range(kv["steps"]))
