@@ -104,6 +104,10 @@ typedef struct sphg_options {
                           -1 = off (one thread per particle, L1-cached global loads) */
   int32_t compute;     /* SPHG_COMPUTE_*; LISTS reads each iteration's list total back
                           to size the lists, so it runs without CUDA graphs or cell tiles */
+  int32_t resort;      /* 1 (default): when at most 8,192 particles changed cell since the
+                          last iteration, re-sort by merging them into the unchanged
+                          (already sorted) rest -- the same stable order as the full radix
+                          sort, which runs otherwise; 0: full radix sort every iteration */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;

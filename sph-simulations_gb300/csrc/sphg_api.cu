@@ -5,10 +5,13 @@
 // here in FP64, and optionally a captured CUDA graph of one step.  Nothing in
 // here computes physics on the host; the host only converts the caller's
 // doubles to the device representation and back.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -166,6 +169,42 @@ int host_cell(double x, double lo, double cs, int cmax) {
 }
 
 
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& f) {
+  const int64_t grain = 1 << 16;
+  int64_t t = std::min<int64_t>((int64_t)std::max(1u, std::thread::hardware_concurrency()), 32);
+  t = std::min<int64_t>(t, (n + grain - 1) / grain);
+  if (t <= 1) {
+    if (n > 0) f(0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const int64_t per = (n + t - 1) / t;
+  for (int64_t k = 1; k < t; ++k) {
+    const int64_t b = k * per, e = std::min(n, b + per);
+    if (b < e) pool.emplace_back([&f, b, e] { f(b, e); });
+  }
+  f(0, std::min(n, per));
+  for (auto& th : pool) th.join();
+}
+
+char* host_stage(sphg_sim* s, size_t bytes) {
+  if (bytes <= s->hstage_bytes) return s->hstage;
+  if (s->hstage) cudaFreeHost(s->hstage);
+  s->hstage = nullptr;
+  s->hstage_bytes = 0;
+  if (cudaMallocHost((void**)&s->hstage, bytes) != cudaSuccess) {
+    s->hstage = nullptr;
+    return nullptr;
+  }
+  s->hstage_bytes = bytes;
+  return s->hstage;
+}
+
+int instance_of(const sphg_sim* s, int64_t i) {
+  const auto& b = s->hbegins;
+  return (int)(std::upper_bound(b.begin(), b.end(), (int32_t)i) - b.begin()) - 1;
+}
+
 }  // namespace sphg_detail
 
 namespace sphg {
@@ -177,16 +216,42 @@ namespace sphg_detail {
 
 // One main-loop iteration.  The force kernel writes the keys of the integrated
 // state, so the key pass only runs on the first iteration after an upload.
-sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false) {
+// With ev (6 events) the phase boundaries are recorded: start, keys, sort,
+// reorder, density, force.
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* ev) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[0], st));
   if (first) SPHG_CUDA(sphg::launch_keys(a, prec, st));
-  // the key writers (key pass / force pass) accumulated the digit histograms
-  SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist));
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[1], st));
+  // the force pass of the previous iteration recorded which slots changed
+  // cell: merge them in when few did (the full sort's kernels then skip)
+  const bool inc = s->movers_on && !first;
+  if (inc) {
+    sphg::MoverArgs m;
+    m.n = s->n;
+    m.keyA = s->keyA;
+    m.keyB = s->keyB;
+    m.mask = s->mmask;
+    m.gsum = s->mgsum;
+    m.wprefix = s->mwprefix;
+    m.movers = s->mlist;
+    m.msorted = s->msorted;
+    m.ctl = s->flags + 3;
+    m.epoch = s->flags + 2;
+    m.keyS = s->keyTmp;
+    m.perm = s->perm;
+    SPHG_CUDA(sphg::launch_movers(m, st));
+  }
+  SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyTmp, s->perm, s->keyA, s->valTmp,
+                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist,
+                                   inc ? s->flags + 3 : nullptr));
   if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[3], st));
+  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->mgsum, 0, sizeof(uint32_t) * s->mgroups, st));
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
     // AssembleNeighborList: count, offsets, fill -- then density and forces over the lists
     SPHG_CUDA(sphg::launch_lists_count_scan(a, prec, s->csr_counts, s->csr_offs, s->csr_sums, st));
@@ -206,14 +271,18 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false) {
     const StepArgs b = s->args();
     SPHG_CUDA(sphg::launch_lists_fill_packed(b, prec, s->csr_offs, s->csr_idx, s->csr_cap, st));
     SPHG_CUDA(sphg::launch_density(b, prec, st, true));
+    if (ev) SPHG_CUDA(cudaEventRecord(ev[4], st));
     SPHG_CUDA(sphg::launch_force(b, prec, sphg::kForceIntegrate, st, true));
   } else if (s->tile_bits) {
     SPHG_CUDA(sphg::launch_tiled(a, prec, false, st));
+    if (ev) SPHG_CUDA(cudaEventRecord(ev[4], st));
     SPHG_CUDA(sphg::launch_tiled(a, prec, true, st));
   } else {
     SPHG_CUDA(sphg::launch_density(a, prec, st));
+    if (ev) SPHG_CUDA(cudaEventRecord(ev[4], st));
     SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
   }
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[5], st));
   return SPHG_OK;
 }
 
@@ -269,6 +338,8 @@ sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p) {
     s->opt.use_graph = 0;  // every iteration reads its list total back
   }
   s->tile_bits = tb > 0 ? tb : 0;
+  // the tile kernels do not record which slots changed cell
+  s->movers_on = s->opt.resort != 0 && s->tile_bits == 0;
   return SPHG_OK;
 }
 
@@ -333,6 +404,14 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     if (s->nbr_slots) {
       s->nbr = A.take<uint32_t>(N * (size_t)s->nbr_slots);
       s->ncount = A.take<uint32_t>(N);
+    }
+    if (s->movers_on) {
+      s->mgroups = sphg::mover_groups((int64_t)N);
+      s->mmask = A.take<uint32_t>((N + 31) / 32);
+      s->mwprefix = A.take<uint32_t>((N + 31) / 32);
+      s->mgsum = A.take<uint32_t>(s->mgroups);
+      s->mlist = A.take<unsigned long long>(sphg::kMoverCap);
+      s->msorted = A.take<unsigned long long>(sphg::kMoverCap);
     }
     if (s->opt.compute == SPHG_COMPUTE_LISTS) {
       s->csr_counts = A.take<int32_t>(N);
@@ -402,6 +481,7 @@ sphg_status destroy_impl(sphg_sim* s) {
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   if (s->arena.base) cudaFree(s->arena.base);
   if (s->csr_idx) cudaFree(s->csr_idx);
+  if (s->hstage) cudaFreeHost(s->hstage);
   delete s;
   return SPHG_OK;
 }
@@ -440,6 +520,7 @@ void sphg_default_options(sphg_options* o) {
   o->use_graph = 1;
   o->tile_bits = 0;
   o->compute = SPHG_COMPUTE_SORTED;
+  o->resort = 1;
 }
 
 const char* sphg_last_error_string(void) { return g_err.c_str(); }
@@ -488,40 +569,48 @@ sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const dou
   if (!s || (s->n > 0 && (!x || !y || !vx || !vy))) return fail(SPHG_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = s->n;
-  std::vector<float2> pos(n), vel(n);
-  std::vector<uint32_t> key;
-  std::vector<int32_t> ids;
-  if (s->opt.precision == SPHG_PRECISION_SPLIT) key.resize(n);
-  for (int inst = 0; inst < s->ninst; ++inst) {
-    const InstDesc& d = s->hdesc[inst];
-    const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
-    const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
-    for (int64_t i = d.begin; i < d.end; ++i) {
-      if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(vx[i]) || !std::isfinite(vy[i]))
-        return fail(SPHG_NONFINITE, "non-finite value in the uploaded state at particle " + std::to_string(i));
-      vel[i] = make_float2((float)vx[i], (float)vy[i]);
-      if (s->opt.precision == SPHG_PRECISION_SPLIT) {
-        int cx = host_cell(x[i], d.lo_xd, d.cs_xd, cmx);
-        int cy = host_cell(y[i], d.lo_yd, d.cs_yd, cmy);
-        uint32_t code = d.order == 0 ? morton_host(cx, cy) : (uint32_t)(cx + cy * d.nx);
-        key[i] = d.cell_base + code;
-        pos[i] = make_float2((float)((x[i] - d.lo_xd) - cx * d.cs_xd),
-                             (float)((y[i] - d.lo_yd) - cy * d.cs_yd));
-      } else {
-        pos[i] = make_float2((float)x[i], (float)y[i]);
-      }
-    }
-  }
   if (n > 0) {
-    SPHG_CUDA(cudaMemcpyAsync(s->posB, pos.data(), n * sizeof(float2), cudaMemcpyHostToDevice, st));
-    SPHG_CUDA(cudaMemcpyAsync(s->velB, vel.data(), n * sizeof(float2), cudaMemcpyHostToDevice, st));
-    if (!key.empty())
-      SPHG_CUDA(cudaMemcpyAsync(s->keyA, key.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    if (s->opt.track_ids) {
-      ids.resize(n);
-      for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
-      SPHG_CUDA(cudaMemcpyAsync(s->idsB, ids.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    }
+    // pinned staging: positions (or split offsets), velocities, split cell keys, creation indices
+    char* stg = host_stage(s, (size_t)n * (sizeof(float2) * 2 + sizeof(uint32_t) + sizeof(int32_t)));
+    if (!stg) return fail(SPHG_OOM, "pinned host staging");
+    float2* pos = reinterpret_cast<float2*>(stg);
+    float2* vel = pos + n;
+    uint32_t* key = reinterpret_cast<uint32_t*>(vel + n);
+    int32_t* ids = reinterpret_cast<int32_t*>(key + n);
+    const bool split = s->opt.precision == SPHG_PRECISION_SPLIT;
+    std::atomic<int64_t> bad{n};
+    parallel_for(n, [&](int64_t b, int64_t e) {
+      int inst = instance_of(s, b);
+      for (int64_t i = b; i < e; ++i) {
+        while (i >= s->hdesc[inst].end) ++inst;
+        const InstDesc& d = s->hdesc[inst];
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(vx[i]) || !std::isfinite(vy[i])) {
+          int64_t cur = bad.load();
+          while (i < cur && !bad.compare_exchange_weak(cur, i)) {
+          }
+          return;
+        }
+        vel[i] = make_float2((float)vx[i], (float)vy[i]);
+        ids[i] = (int32_t)i;
+        if (split) {
+          const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
+          const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
+          int cx = host_cell(x[i], d.lo_xd, d.cs_xd, cmx);
+          int cy = host_cell(y[i], d.lo_yd, d.cs_yd, cmy);
+          uint32_t code = d.order == 0 ? morton_host(cx, cy) : (uint32_t)(cx + cy * d.nx);
+          key[i] = d.cell_base + code;
+          pos[i] = make_float2((float)((x[i] - d.lo_xd) - cx * d.cs_xd), (float)((y[i] - d.lo_yd) - cy * d.cs_yd));
+        } else {
+          pos[i] = make_float2((float)x[i], (float)y[i]);
+        }
+      }
+    });
+    if (bad.load() < n)
+      return fail(SPHG_NONFINITE, "non-finite value in the uploaded state at particle " + std::to_string(bad.load()));
+    SPHG_CUDA(cudaMemcpyAsync(s->posB, pos, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    SPHG_CUDA(cudaMemcpyAsync(s->velB, vel, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    if (split) SPHG_CUDA(cudaMemcpyAsync(s->keyA, key, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    if (s->opt.track_ids) SPHG_CUDA(cudaMemcpyAsync(s->idsB, ids, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     // digit histograms of the next sort restart with the uploaded state
     SPHG_CUDA(cudaMemsetAsync(s->scratch, 0, sizeof(uint32_t) * 4 * 256, st));
     SPHG_CUDA(cudaStreamSynchronize(st));
@@ -552,45 +641,54 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = s->n;
   if (n == 0) return SPHG_OK;
-  std::vector<float2> pos(n), acc;
-  std::vector<float4> velp(n);
-  std::vector<float> r(n);
-  std::vector<uint32_t> key(n);
-  if (fx || fy) {
+  const bool forces = fx || fy;
+  char* stg = host_stage(s, (size_t)n * (sizeof(float2) * 2 + sizeof(float4) + sizeof(float) + sizeof(uint32_t)));
+  if (!stg) return fail(SPHG_OOM, "pinned host staging");
+  float4* velp = reinterpret_cast<float4*>(stg);
+  float2* pos = reinterpret_cast<float2*>(velp + n);
+  float2* acc = pos + n;
+  float* r = reinterpret_cast<float*>(acc + n);
+  uint32_t* key = reinterpret_cast<uint32_t*>(r + n);
+  const bool split = s->opt.precision == SPHG_PRECISION_SPLIT;
+  if (forces) {
     SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
-    acc.resize(n);
-    SPHG_CUDA(cudaMemcpyAsync(acc.data(), s->acc, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaMemcpyAsync(acc, s->acc, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
   }
-  SPHG_CUDA(cudaMemcpyAsync(pos.data(), s->posA, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
-  SPHG_CUDA(cudaMemcpyAsync(velp.data(), s->velpA, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  SPHG_CUDA(cudaMemcpyAsync(r.data(), s->rho, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-  SPHG_CUDA(cudaMemcpyAsync(key.data(), s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  if (x || y) SPHG_CUDA(cudaMemcpyAsync(pos, s->posA, n * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  if (vx || vy) SPHG_CUDA(cudaMemcpyAsync(velp, s->velpA, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  if (rho) SPHG_CUDA(cudaMemcpyAsync(r, s->rho, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  if (split && (x || y))
+    SPHG_CUDA(cudaMemcpyAsync(key, s->keyA, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   if (ids && s->opt.track_ids)
     SPHG_CUDA(cudaMemcpyAsync(ids, s->idsA, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
   if (ids && !s->opt.track_ids)
     for (int64_t i = 0; i < n; ++i) ids[i] = -1;
-  for (int inst = 0; inst < s->ninst; ++inst) {
-    const InstDesc& d = s->hdesc[inst];
-    for (int64_t i = d.begin; i < d.end; ++i) {
-      double px = pos[i].x, py = pos[i].y;
-      if (s->opt.precision == SPHG_PRECISION_SPLIT) {
-        int cx, cy;
-        uint32_t code = key[i] - d.cell_base;
-        if (d.order == 0) demorton_host(code, cx, cy);
-        else { cx = (int)(code % (uint32_t)d.nx); cy = (int)(code / (uint32_t)d.nx); }
-        px = d.lo_xd + cx * d.cs_xd + px;
-        py = d.lo_yd + cy * d.cs_yd + py;
+  parallel_for(n, [&](int64_t b, int64_t e) {
+    int inst = instance_of(s, b);
+    for (int64_t i = b; i < e; ++i) {
+      while (i >= s->hdesc[inst].end) ++inst;
+      const InstDesc& d = s->hdesc[inst];
+      if (x || y) {
+        double px = pos[i].x, py = pos[i].y;
+        if (split) {
+          int cx, cy;
+          const uint32_t code = key[i] - d.cell_base;
+          if (d.order == 0) demorton_host(code, cx, cy);
+          else { cx = (int)(code % (uint32_t)d.nx); cy = (int)(code / (uint32_t)d.nx); }
+          px = d.lo_xd + cx * d.cs_xd + px;
+          py = d.lo_yd + cy * d.cs_yd + py;
+        }
+        if (x) x[i] = px;
+        if (y) y[i] = py;
       }
-      if (x) x[i] = px;
-      if (y) y[i] = py;
       if (vx) vx[i] = velp[i].x;
       if (vy) vy[i] = velp[i].y;
       if (rho) rho[i] = r[i];
       if (fx) fx[i] = acc[i].x;
       if (fy) fy[i] = acc[i].y;
     }
-  }
+  });
   return SPHG_OK;
 }
 
@@ -598,8 +696,11 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream) {
   if (!s || !out) return fail(SPHG_INVALID_ARG, "null argument");
   if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
   cudaStream_t st = (cudaStream_t)stream;
-  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials,
-                                     s->diag_chunks, s->diag_out, st));
+  int64_t max_n = 0;
+  for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
+  const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks,
+                                     s->diag_out, st));
   SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst,
                             cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
@@ -778,30 +879,12 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) SPHG_CUDA(cudaEventCreate(&ev[i]));
-  const StepArgs a = s->args();
-  const int prec = s->opt.precision;
-  sphg_status res = SPHG_OK;
-  auto run = [&]() -> sphg_status {
-    SPHG_CUDA(cudaEventRecord(ev[0], st));
-    SPHG_CUDA(cudaEventRecord(ev[1], st));
-    SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyA, s->perm, s->keyTmp, s->valTmp,
-                                     s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist));
-    if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
-    SPHG_CUDA(cudaEventRecord(ev[2], st));
-    if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
-    SPHG_CUDA(sphg::launch_reorder(a, st));
-    SPHG_CUDA(cudaEventRecord(ev[3], st));
-    if (s->tile_bits) SPHG_CUDA(sphg::launch_tiled(a, prec, false, st));
-    else SPHG_CUDA(sphg::launch_density(a, prec, st));
-    SPHG_CUDA(cudaEventRecord(ev[4], st));
-    if (s->tile_bits) SPHG_CUDA(sphg::launch_tiled(a, prec, true, st));
-    else SPHG_CUDA(sphg::launch_force(a, prec, sphg::kForceIntegrate, st));
-    SPHG_CUDA(cudaEventRecord(ev[5], st));
-    SPHG_CUDA(cudaEventSynchronize(ev[5]));
-    for (int i = 0; i < 5; ++i) SPHG_CUDA(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
-    return SPHG_OK;
-  };
-  res = run();
+  sphg_status res = enqueue_step(s, st, false, ev);
+  if (res == SPHG_OK) {
+    cudaError_t e = cudaEventSynchronize(ev[5]);
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    if (e != cudaSuccess) res = fail(SPHG_CUDA_ERROR, std::string("profile events: ") + cudaGetErrorString(e));
+  }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   return res;
 }
@@ -810,8 +893,9 @@ int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
   // the sort's histogram kernel + radix passes + reorder + density + force
-  // (+ list count, three scan kernels and list fill in the lists mode)
-  return passes + 4 + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
+  // (+ the three incremental re-sort kernels; + list count, three scan kernels
+  // and list fill in the lists mode)
+  return passes + 4 + (s->movers_on ? 3 : 0) + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
 }
 
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

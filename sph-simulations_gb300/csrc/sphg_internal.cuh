@@ -4,11 +4,13 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include <cuda_runtime.h>
 
 #include "../../include/sphg.h"
+#include "sphg_movers.cuh"
 #include "sphg_step.cuh"
 
 using sphg::InstDesc;
@@ -62,12 +64,20 @@ struct sphg_sim {
   int64_t *csr_offs = nullptr, *csr_sums = nullptr;
   uint32_t* csr_idx = nullptr;
   int64_t csr_cap = 0, csr_total = 0;
+  // incremental re-sort: mover bits and group counts written by the force pass
+  bool movers_on = false;
+  uint32_t *mmask = nullptr, *mgsum = nullptr, *mwprefix = nullptr;
+  unsigned long long *mlist = nullptr, *msorted = nullptr;
+  int mgroups = 0;
   size_t cap_n = 0;             // arena capacity (particles)
   uint64_t cap_keys = 0;        // arena capacity (cell keys)
   int cap_inst = 0;             // arena capacity (instances)
   int force_batched = 0;        // always use the per-instance-descriptor kernels
   int tile_bits = 0, tile_cap = 0, tile_grid = 0;
   bool uploaded = false, preloop_done = false;
+  // pinned host staging of upload/download (grows on demand)
+  char* hstage = nullptr;
+  size_t hstage_bytes = 0;
   // CUDA graph of one step
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -109,6 +119,9 @@ struct sphg_sim {
     a.nbr_slots = nbr_slots;
     a.csr_offs = csr_offs;
     a.csr_idx = csr_idx;
+    a.keyS = keyTmp;
+    a.mover_mask = movers_on ? mmask : nullptr;
+    a.mover_gsum = movers_on ? mgsum : nullptr;
     return a;
   }
 };
@@ -134,9 +147,16 @@ sphg_status fail(sphg_status st, const std::string& msg);
 sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64_t cell_base,
                       InstDesc& d, uint64_t& span);
 int host_cell(double x, double lo, double cs, int cmax);
+// f(begin, end) over [0, n) split across host threads (one thread for small n).
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& f);
+// Pinned host staging of at least `bytes` owned by the handle (nullptr: out of memory).
+char* host_stage(sphg_sim* s, size_t bytes);
+// Instance holding particle i (instances are contiguous in particle order).
+int instance_of(const sphg_sim* s, int64_t i);
 uint32_t morton_host(uint32_t x, uint32_t y);
 void demorton_host(uint32_t z, int& x, int& y);
-sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first);
+// One main-loop iteration on st; ev (6 events, optional) records the phase boundaries.
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false, cudaEvent_t* ev = nullptr);
 
 struct Layout {
   std::vector<InstDesc> desc;

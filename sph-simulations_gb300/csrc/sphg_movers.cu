@@ -1,0 +1,209 @@
+// sphg_movers.cu -- incremental re-sort of a nearly sorted state.
+//
+// Between two main-loop iterations a particle moves a small fraction of a
+// cell, so almost every particle keeps its cell key.  The stable sort of the
+// new keys (GenericNeighborSearch::SortParticleIds,
+// core/alg/GenericNeighborSearch.h:69-76, with ties in previous-slot order)
+// is then a merge of two sorted sequences:
+//   * stayers: slots whose key did not change -- already in (key, slot) order,
+//     because the current state is sorted;
+//   * movers: slots whose key changed -- few, sorted here in one CTA.
+// A stayer's new position is its rank among stayers plus the number of movers
+// ordered before it; a mover's is its rank among movers plus the number of
+// stayers ordered before it.  The force pass records which slots moved (one
+// bit per slot, and a count per group of 65,536 slots); when more than
+// kMoverCap slots moved, the full radix sort runs instead (its kernels read the
+// same decision word and skip themselves otherwise).
+//
+// Kernels: movers_compact (mover list in slot order, movers before each word,
+// decision), movers_sort_place (bitonic sort of the movers in shared memory,
+// their final positions), stayers_place (every stayer's final position).
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "sphg_movers.cuh"
+
+namespace sphg {
+
+namespace {
+
+constexpr int kCompactThreads = 256;
+constexpr int kCompactWords = 8;  // words per thread: 256 x 8 words = one group of 65,536 slots
+constexpr int kPlaceThreads = 1024;
+constexpr int kStayThreads = 256;
+
+__device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p, uint32_t m) {
+  if (p >= a.n) return m;
+  const int64_t w = p >> 5;
+  const uint32_t below = (1u << (p & 31)) - 1u;
+  return a.wprefix[w] + __popc(a.mask[w] & below);
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+  return t;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
+  __shared__ uint32_t red[kCompactThreads / 32];
+  __shared__ uint32_t scan[kCompactThreads / 32];
+  const int g = blockIdx.x;
+  const int ngroups = (int)gridDim.x;
+  // movers in all groups, and in the groups before this one
+  uint32_t pre = 0, tot = 0;
+  for (int k = threadIdx.x; k < ngroups; k += blockDim.x) {
+    const uint32_t v = a.gsum[k];
+    tot += v;
+    if (k < g) pre += v;
+  }
+  tot = block_sum(tot, red);
+  pre = block_sum(pre, red);
+  const bool inc = tot <= (uint32_t)kMoverCap;
+  if (g == 0 && threadIdx.x == 0) {
+    a.ctl[0] = inc ? 1u : 0u;
+    a.ctl[1] = tot;
+    if (inc) *a.epoch += 1u;  // the step epoch the skipped radix sort would have bumped
+  }
+  if (!inc) return;
+  const int64_t nwords = (a.n + 31) >> 5;
+  const int64_t w0 = ((int64_t)g << (kGroupShift - 5)) + (int64_t)threadIdx.x * kCompactWords;
+  uint32_t mw[kCompactWords];
+  uint32_t c = 0;
+#pragma unroll
+  for (int q = 0; q < kCompactWords; ++q) {
+    mw[q] = (w0 + q < nwords) ? a.mask[w0 + q] : 0u;
+    c += __popc(mw[q]);
+  }
+  // exclusive scan of the per-thread counts
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  uint32_t x = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) scan[wp] = x;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (int k = 0; k < wp; ++k) wbase += scan[k];
+  uint32_t r = pre + wbase + x - c;
+#pragma unroll
+  for (int q = 0; q < kCompactWords; ++q) {
+    const int64_t w = w0 + q;
+    if (w >= nwords) break;
+    a.wprefix[w] = r;
+    uint32_t bits = mw[q];
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const uint32_t slot = (uint32_t)((w << 5) + b);
+      a.movers[r] = ((uint64_t)a.keyB[slot] << 32) | slot;
+      ++r;
+    }
+  }
+}
+
+// lower bound of (key, slot) among the slots' (keyA[s], s): slots are sorted by it
+__device__ __forceinline__ int64_t slots_before(const MoverArgs& a, uint32_t k, uint32_t sl) {
+  int64_t lo = 0, hi = a.n;
+  while (lo < hi) {  // first slot with keyA >= k
+    const int64_t mid = (lo + hi) >> 1;
+    if (a.keyA[mid] < k) lo = mid + 1;
+    else hi = mid;
+  }
+  const int64_t first = lo;
+  hi = a.n;
+  while (lo < hi) {  // first slot with keyA > k
+    const int64_t mid = (lo + hi) >> 1;
+    if (a.keyA[mid] <= k) lo = mid + 1;
+    else hi = mid;
+  }
+  const int64_t last = lo;
+  const int64_t s = (int64_t)sl;
+  return s < first ? first : (s > last ? last : s);
+}
+
+__global__ void __launch_bounds__(kPlaceThreads) movers_sort_place(MoverArgs a) {
+  extern __shared__ unsigned long long sm[];
+  if (!a.ctl[0]) return;
+  const uint32_t m = a.ctl[1];
+  if (m == 0) return;
+  uint32_t cap = 2;
+  while (cap < m) cap <<= 1;
+  for (uint32_t r = threadIdx.x; r < cap; r += blockDim.x)
+    sm[r] = r < m ? (unsigned long long)a.movers[r] : ~0ull;
+  __syncthreads();
+  // bitonic sort, ascending on (key << 32 | slot)
+  for (uint32_t k = 2; k <= cap; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t t = threadIdx.x; t < (cap >> 1); t += blockDim.x) {
+        const uint32_t i0 = 2 * t - (t & (j - 1));  // lower index of the pair
+        const uint32_t i1 = i0 + j;
+        const bool up = (i0 & k) == 0;
+        const unsigned long long u = sm[i0], v = sm[i1];
+        if ((u > v) == up) {
+          sm[i0] = v;
+          sm[i1] = u;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (uint32_t r = threadIdx.x; r < m; r += blockDim.x) {
+    const unsigned long long v = sm[r];
+    const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
+    a.msorted[r] = v;
+    const int64_t p = slots_before(a, k, sl);
+    const int64_t fin = (int64_t)r + (p - (int64_t)movers_before(a, p, m));
+    a.keyS[fin] = k;
+    a.perm[fin] = sl;
+  }
+}
+
+__global__ void __launch_bounds__(kStayThreads) stayers_place(MoverArgs a) {
+  if (!a.ctl[0]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  if ((a.mask[i >> 5] >> (i & 31)) & 1u) return;
+  const uint32_t m = a.ctl[1];
+  const uint32_t k = a.keyA[i];
+  const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
+  uint32_t lo = 0, hi = m;  // movers ordered before this stayer
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((unsigned long long)a.msorted[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  const int64_t fin = i - (int64_t)movers_before(a, i, m) + lo;
+  a.keyS[fin] = k;
+  a.perm[fin] = (uint32_t)i;
+}
+
+}  // namespace
+
+int mover_groups(int64_t n) { return (int)((n + (1 << kGroupShift) - 1) >> kGroupShift); }
+
+cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(movers_sort_place, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kMoverCap * (int)sizeof(unsigned long long));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  movers_compact<<<mover_groups(a.n), kCompactThreads, 0, st>>>(a);
+  movers_sort_place<<<1, kPlaceThreads, kMoverCap * sizeof(unsigned long long), st>>>(a);
+  stayers_place<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace sphg

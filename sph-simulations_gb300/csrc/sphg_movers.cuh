@@ -1,0 +1,31 @@
+// sphg_movers.cuh -- launch interface of the incremental re-sort (sphg_movers.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphg {
+
+constexpr int kGroupShift = 16;   // slots per mover group count: 65,536
+constexpr int kMoverCap = 8192;   // largest mover set sorted in one CTA (64 KB of shared memory)
+
+struct MoverArgs {
+  int64_t n;
+  const uint32_t* keyA;    // sorted keys of the current state, slot order
+  const uint32_t* keyB;    // keys of the integrated state, per slot
+  const uint32_t* mask;    // [ceil(n/32)] bit s%32 of word s/32: slot s changed key
+  const uint32_t* gsum;    // [mover_groups(n)] changed slots per group of 65,536 slots
+  uint32_t* wprefix;       // [ceil(n/32)] changed slots before each word
+  unsigned long long* movers;   // [kMoverCap] key << 32 | slot, slot order
+  unsigned long long* msorted;  // [kMoverCap] the same, ascending
+  uint32_t* ctl;           // [0] = 1 when the incremental path ran, [1] = changed slots
+  uint32_t* epoch;         // step epoch of the cell-range table
+  uint32_t* keyS;          // out: sorted keys
+  uint32_t* perm;          // out: previous slot of each sorted position
+};
+
+int mover_groups(int64_t n);
+// movers_compact, movers_sort_place, stayers_place; when more than kMoverCap
+// slots changed they do nothing and leave ctl[0] = 0 for the full sort.
+cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st);
+
+}  // namespace sphg

@@ -52,7 +52,9 @@ constexpr int kHistPerThread = 16;
 
 __global__ void __launch_bounds__(kSortThreads) sort_hist_all(const uint32_t* __restrict__ keys,
                                                               int64_t n, int passes,
-                                                              uint32_t* __restrict__ ghist) {
+                                                              uint32_t* __restrict__ ghist,
+                                                              const uint32_t* skip) {
+  if (skip && *skip) return;
   __shared__ uint32_t h[kMaxPasses][kRadix];
   for (int p = 0; p < kMaxPasses; ++p) h[p][threadIdx.x] = 0;
   __syncthreads();
@@ -97,7 +99,8 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int pass,
     const uint32_t* __restrict__ ghist, uint32_t* tile_counter, uint32_t* lookback,
-    uint32_t* err, uint32_t* epoch) {
+    uint32_t* err, uint32_t* epoch, const uint32_t* skip) {
+  if (skip && *skip) return;  // the incremental re-sort handled this step
   __shared__ uint32_t s_tile;
   __shared__ uint32_t base_s[kRadix];
   __shared__ uint32_t running[kRadix];
@@ -222,7 +225,8 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass(
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
-                             cudaStream_t stream, uint32_t* epoch, const uint32_t* hist) {
+                             cudaStream_t stream, uint32_t* epoch, const uint32_t* hist,
+                             const uint32_t* skip) {
   if (n <= 0) return cudaSuccess;
   const int passes = passes_for(bits);
   // big inputs: 4096-key tiles halve the look-back chain; small ones: 2048 for parallelism
@@ -247,7 +251,7 @@ cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
   if (!hist) {
     const int64_t hchunks = (n + kSortThreads * kHistPerThread - 1) / (kSortThreads * kHistPerThread);
     const int hist_blocks = (int)(hchunks < 608 ? hchunks : 608);
-    sort_hist_all<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, n, passes, ghist);
+    sort_hist_all<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, n, passes, ghist, skip);
     hist = ghist;
   }
   const uint32_t* kin = keys_in;
@@ -259,11 +263,11 @@ cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
     if (items == 16)
       sort_pass<16><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, p, hist, tile_counter,
                                                          lookback + (size_t)p * kRadix * ntiles, err,
-                                                         p == 0 ? epoch : nullptr);
+                                                         p == 0 ? epoch : nullptr, skip);
     else
       sort_pass<8><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, ko, vo, n, p, hist, tile_counter,
                                                         lookback + (size_t)p * kRadix * ntiles, err,
-                                                        p == 0 ? epoch : nullptr);
+                                                        p == 0 ? epoch : nullptr, skip);
     kin = ko;
     vin = vo;
   }

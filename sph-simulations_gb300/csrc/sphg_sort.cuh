@@ -22,11 +22,13 @@ uint32_t* sort_error_word(uint32_t* scratch);
 // increments *epoch once (the step epoch of the cell-range table).  hist, when
 // not null, holds the digit histograms of all passes already ([4][256], digit
 // d of pass p at p*256 + d, summed over all keys); otherwise they are computed.
+// When *skip (device word, read by the kernels) is non-zero the kernels return
+// at once: the step's incremental re-sort produced the result instead.
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
                              cudaStream_t stream, uint32_t* epoch = nullptr,
-                             const uint32_t* hist = nullptr);
+                             const uint32_t* hist = nullptr, const uint32_t* skip = nullptr);
 constexpr int kSortMaxPasses = 4;
 
 }  // namespace sphg

@@ -77,15 +77,16 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const uint32_t src = a.perm[i];
-  const uint32_t k = a.keyA[i];
+  const uint32_t k = a.keyS[i];
+  a.keyA[i] = k;
   float2 p = a.posB[src];
   float2 v = a.velB[src];
   a.posA[i] = p;
   a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
   if (a.track_ids) a.idsA[i] = a.idsB[src];
   uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
-  const uint32_t kprev = i > 0 ? a.keyA[i - 1] : kNoIndex;
-  const uint32_t knext = i + 1 < a.n ? a.keyA[i + 1] : kNoIndex;
+  const uint32_t kprev = i > 0 ? a.keyS[i - 1] : kNoIndex;
+  const uint32_t knext = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;
   if (k != kprev) {
     r[4 * (size_t)k] = (uint32_t)i;
     r[4 * (size_t)k + 2] = *a.epoch;
@@ -199,6 +200,14 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   uint32_t key = 0;
   if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, bd, bj);
   if (hist) histogram_keys(a, hs, valid, key);
+  if (MODE == kForceIntegrate && a.mover_mask) {
+    // slots whose cell key changed, for the incremental re-sort (a warp holds 32 consecutive slots)
+    const unsigned moved = __ballot_sync(0xffffffffu, valid && key != a.keyA[i]);
+    if ((threadIdx.x & 31) == 0 && valid) {
+      a.mover_mask[i >> 5] = moved;
+      if (moved) atomicAdd(a.mover_gsum + (i >> 16), (uint32_t)__popc(moved));
+    }
+  }
 }
 
 // Forces on particle i; in integrate mode also the update and the new key
@@ -313,6 +322,26 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Per (chunk, instance) block: FP64 partial sums of one contiguous piece of the
+// instance, a fixed-shape block reduction (deterministic for a given chunk count).
+__device__ __forceinline__ void block_reduce6(double (&v)[6], double (*sh)[kDiagThreads / 32]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) v[f] = (f == 1) ? warp_max(v[f]) : warp_sum(v[f]);
+  if (lane == 0) {
+#pragma unroll
+    for (int f = 0; f < 6; ++f) sh[f][w] = v[f];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int f = threadIdx.x;
+    double acc = sh[f][0];
+    for (int k = 1; k < kDiagThreads / 32; ++k) acc = (f == 1) ? fmax(acc, sh[f][k]) : acc + sh[f][k];
+    sh[f][0] = acc;
+  }
+  __syncthreads();
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, int chunks,
                                                                   double* partials) {
@@ -322,16 +351,16 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
   const int64_t per = (cnt + chunks - 1) / chunks;
   const int64_t b = d.begin + per * blockIdx.x;
   const int64_t e = min((int64_t)d.end, b + per);
-  double ek = 0, vmax = 0, inside = 0, px = 0, py = 0, bad = 0;
+  double v[6] = {0, 0, 0, 0, 0, 0};  // E_k, max |v|^2, inside, sum m vx, sum m vy, non-finite
   for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-    const float4 v = a.velpA[i];
+    const float4 vel = a.velpA[i];
     const float2 p = a.posA[i];
-    const double vx = v.x, vy = v.y;
+    const double vx = vel.x, vy = vel.y;
     const double n2 = vx * vx + vy * vy;
-    ek += 0.5 * n2 * d.mass_d;
-    vmax = fmax(vmax, n2);
-    px += d.mass_d * vx;
-    py += d.mass_d * vy;
+    v[0] += 0.5 * n2 * d.mass_d;
+    v[1] = fmax(v[1], n2);
+    v[3] += d.mass_d * vx;
+    v[4] += d.mass_d * vy;
     double x = p.x, y = p.y;
     if (PREC == 1) {
       int cx, cy;
@@ -341,38 +370,27 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
     }
     const bool fin = isfinite(x) && isfinite(y) && isfinite(vx) && isfinite(vy) &&
                      isfinite(a.rho[i]);
-    inside += (fin && !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd)) ? 1.0 : 0.0;
-    bad += fin ? 0.0 : 1.0;
+    v[2] += (fin && !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd)) ? 1.0 : 0.0;
+    v[5] += fin ? 0.0 : 1.0;
   }
   __shared__ double sh[6][kDiagThreads / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  ek = warp_sum(ek);
-  vmax = warp_max(vmax);
-  inside = warp_sum(inside);
-  px = warp_sum(px);
-  py = warp_sum(py);
-  bad = warp_sum(bad);
-  if (lane == 0) {
-    sh[0][w] = ek; sh[1][w] = vmax; sh[2][w] = inside; sh[3][w] = px; sh[4][w] = py; sh[5][w] = bad;
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    double acc = 0;
-    for (int k = 0; k < kDiagThreads / 32; ++k)
-      acc = (threadIdx.x == 1) ? fmax(acc, sh[1][k]) : acc + sh[threadIdx.x][k];
-    partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = acc;
-  }
+  block_reduce6(v, sh);
+  if (threadIdx.x < 6) partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void step_diag_final(int ninst, int chunks, const double* partials, double* out) {
-  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
-  if (inst >= ninst) return;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int c = 0; c < chunks; ++c) {
+// One block per instance: strided partials per thread, then the same fixed-shape reduction.
+__global__ void __launch_bounds__(kDiagThreads) step_diag_final(int chunks, const double* partials,
+                                                                double* out) {
+  const int inst = blockIdx.x;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
     const double* p = partials + ((size_t)inst * chunks + c) * 6;
-    for (int f = 0; f < 6; ++f) acc[f] = (f == 1) ? fmax(acc[f], p[f]) : acc[f] + p[f];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) v[f] = (f == 1) ? fmax(v[f], p[f]) : v[f] + p[f];
   }
-  for (int f = 0; f < 6; ++f) out[inst * 6 + f] = acc[f];
+  __shared__ double sh[6][kDiagThreads / 32];
+  block_reduce6(v, sh);
+  if (threadIdx.x < 6) out[inst * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // ---------------------------------------------------------------- stand-alone keys
@@ -437,10 +455,10 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
   return cudaGetLastError();
 }
 
-int diag_chunks(int64_t max_inst_n) {
-  int64_t c = (max_inst_n + 4095) / 4096;
+int diag_chunks(int64_t max_inst_n, int cap) {
+  int64_t c = (max_inst_n + 1023) / 1024;  // about four particles per thread
   if (c < 1) c = 1;
-  if (c > 256) c = 256;
+  if (c > cap) c = cap;
   return (int)c;
 }
 
@@ -449,7 +467,7 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
   dim3 g(chunks, a.ninst);
   if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
   else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  step_diag_final<<<blocks_for(a.ninst, 128), 128, 0, s>>>(a.ninst, chunks, partials, out);
+  step_diag_final<<<a.ninst, kDiagThreads, 0, s>>>(chunks, partials, out);
   return cudaGetLastError();
 }
 

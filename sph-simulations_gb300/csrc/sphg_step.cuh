@@ -21,7 +21,8 @@ struct StepArgs {
   float2* posA;
   float4* velpA;               // (vx, vy, p/rho^2, 1/rho)
   float* rho;
-  uint32_t* keyA;              // sorted global keys
+  uint32_t* keyA;              // sorted global keys (written by the reorder)
+  const uint32_t* keyS;        // sort output: sorted keys, read by the reorder
   uint4* ranges;               // [total keys] {start, end, epoch, 0}
   const uint32_t* epoch;       // current step's epoch (bumped by the sort)
   int32_t* idsA;
@@ -37,6 +38,8 @@ struct StepArgs {
   int nbr_slots;
   const int64_t* csr_offs;     // [n+1] CSR neighbour lists of this iteration (lists mode)
   const uint32_t* csr_idx;     // j << 5 | tag entries, self included, list order
+  uint32_t* mover_mask;        // [ceil(n/32)] force pass: bit per slot whose key changed (or null)
+  uint32_t* mover_gsum;        // [groups of 65,536 slots] changed slots per group (zeroed before)
   uint32_t* ghist;             // digit histograms of the next sort (accumulated by the key writers)
   int key_passes;              // radix passes of the next sort
   uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
@@ -66,7 +69,9 @@ cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int
 // final sum; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx, sum m vy, nonfinite.
 cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
                                double* out, cudaStream_t s);
-int diag_chunks(int64_t max_inst_n);
+// Diagnostics chunks of the largest instance (at most cap; the partial buffer
+// holds ninst x cap x 6 doubles).
+int diag_chunks(int64_t max_inst_n, int cap = 1024);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
                cudaStream_t st, std::string* err, bool encoded = false);

@@ -41,7 +41,7 @@ class Params(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
-                ("compute", ctypes.c_int32)]
+                ("compute", ctypes.c_int32), ("resort", ctypes.c_int32)]
 
 
 _lib = None
@@ -127,9 +127,11 @@ def params(**kw):
     return p
 
 
-def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None):
+def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None, resort=None):
     o = Options()
     lib().sphg_default_options(ctypes.byref(o))
+    if resort is not None:
+        o.resort = int(resort)
     o.precision = precision
     o.track_ids = track_ids
     o.use_graph = use_graph

@@ -676,3 +676,39 @@ def test_encoded_lists_round_trip(golden):
         torch.cuda.synchronize()
         assert (d_enc.cpu().numpy() == want).all()
         assert (d_dec.cpu().numpy() == a_).all()
+
+
+# ---------------------------------------------------------------- incremental re-sort
+@pytest.mark.parametrize("prec", ["plain", "split"])
+@pytest.mark.parametrize("vel", [0.3, 400.0])
+def test_incremental_resort_equals_full_sort_bitwise(prec, vel):
+    """resort=1 merges the particles that changed cell into the rest; it must give
+    the full radix sort's order and therefore the same bits.  vel=400 moves more
+    than 8,192 particles a step, so the device falls back to the full sort."""
+    S = _sphg()
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    x, y, vx, vy = jittered(160, 120, 0.005, seed=31, vel=vel)
+    prm = S.params(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.8, 0.6))
+    outs = []
+    for resort in (1, 0):
+        sim = S.Sim(prm, len(x), S.options(precision=P, resort=resort))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        moved = []
+        for _ in range(6):
+            before = sim.debug(S.DBG_KEYS).copy()
+            nxt = sim.debug(S.DBG_UNSORTED_KEYS)
+            moved.append(int((before != nxt).sum()))
+            sim.step(4)
+        o = sim.download()
+        o["keys"] = sim.debug(S.DBG_KEYS)
+        o["perm"] = sim.debug(S.DBG_PERM)
+        outs.append((o, moved))
+        sim.close()
+    (a, moved), (b, _) = outs
+    if vel < 1:
+        assert 0 < max(moved) <= 8192
+    else:
+        assert min(moved) > 8192
+    for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids", "keys", "perm"):
+        assert np.array_equal(a[f], b[f], equal_nan=True), f
