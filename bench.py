@@ -247,8 +247,15 @@ def run_gpu(args):
     value = n * world * args.steps / (total_ms * 1e-3)
 
     # ---- per-phase profile (CUDA events between the kernels of one iteration)
-    phases = np.array([sim.profile_step(stream=sptr) for _ in range(20)])
+    phases, resort = [], []
+    for _ in range(20):
+        phases.append(sim.profile_step(stream=sptr))
+        resort.append(sim.debug(sphg.DBG_RESORT, stream=sptr).tolist())
+    phases = np.array(phases)
     phase_ms = phases.mean(axis=0).tolist()
+    resort = np.array(resort)
+    resort_out = {"incremental_fraction": float(resort[:, 0].mean()),
+                  "cell_changes_per_step": float(resort[:, 1].mean())}
     diag = sim.diagnostics(stream=sptr)
     launches = sim.launches_per_step() * args.steps
     sim.close()
@@ -342,7 +349,7 @@ def run_gpu(args):
             "data": "synthetic: seeded jittered-lattice initial states (no dataset)",
             "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk, "phases_ms": phases_out,
-            "dominant_phase": dominant,
+            "dominant_phase": dominant, "resort": resort_out,
             "diagnostics_after": {"E_k": float(diag[:, 0].sum()), "max_v2": float(diag[:, 1].max()),
                                   "inside": float(diag[:, 2].sum()), "nonfinite": float(diag[:, 5].sum())},
         }

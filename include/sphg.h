@@ -145,7 +145,9 @@ enum {
   SPHG_DBG_PERM = 1,        /* int32[n]  slot before the last sort of each slot */
   SPHG_DBG_UNSORTED_KEYS = 2,/* int32[n] keys of the integrated state awaiting the next sort */
   SPHG_DBG_POS_NEXT = 3,    /* double[2n] integrated positions awaiting the next sort */
-  SPHG_DBG_VEL_NEXT = 4     /* double[2n] integrated velocities awaiting the next sort */
+  SPHG_DBG_VEL_NEXT = 4,    /* double[2n] integrated velocities awaiting the next sort */
+  SPHG_DBG_RESORT = 5       /* int32[2]  last iteration: 1 if the incremental re-sort ran
+                               (0: the full radix sort), particles that changed cell */
 };
 sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream);
 

@@ -200,6 +200,12 @@ char* host_stage(sphg_sim* s, size_t bytes) {
   return s->hstage;
 }
 
+float split_offset(double o, double cs) {
+  float r = (float)o;
+  if ((double)r >= cs) r = std::nextafter(r, 0.0f);  // stay inside the cell after rounding
+  return r;
+}
+
 int instance_of(const sphg_sim* s, int64_t i) {
   const auto& b = s->hbegins;
   return (int)(std::upper_bound(b.begin(), b.end(), (int32_t)i) - b.begin()) - 1;
@@ -599,7 +605,8 @@ sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const dou
           int cy = host_cell(y[i], d.lo_yd, d.cs_yd, cmy);
           uint32_t code = d.order == 0 ? morton_host(cx, cy) : (uint32_t)(cx + cy * d.nx);
           key[i] = d.cell_base + code;
-          pos[i] = make_float2((float)((x[i] - d.lo_xd) - cx * d.cs_xd), (float)((y[i] - d.lo_yd) - cy * d.cs_yd));
+          pos[i] = make_float2(split_offset((x[i] - d.lo_xd) - cx * d.cs_xd, d.cs_xd),
+                               split_offset((y[i] - d.lo_yd) - cy * d.cs_yd, d.cs_yd));
         } else {
           pos[i] = make_float2((float)x[i], (float)y[i]);
         }
@@ -724,6 +731,15 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
     return SPHG_OK;
   };
   switch (which) {
+    case SPHG_DBG_RESORT: {
+      uint32_t c[2] = {0, 0};
+      if (s->movers_on) {
+        SPHG_CUDA(cudaMemcpyAsync(c, s->flags + 3, sizeof(c), cudaMemcpyDeviceToHost, st));
+        SPHG_CUDA(cudaStreamSynchronize(st));
+      }
+      std::memcpy(host, c, sizeof(c));
+      return SPHG_OK;
+    }
     case SPHG_DBG_KEYS: return local_keys(s->keyA);
     case SPHG_DBG_UNSORTED_KEYS: return local_keys(s->keyB);
     case SPHG_DBG_PERM:

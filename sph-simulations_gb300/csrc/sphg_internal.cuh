@@ -151,6 +151,8 @@ int host_cell(double x, double lo, double cs, int cmax);
 void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& f);
 // Pinned host staging of at least `bytes` owned by the handle (nullptr: out of memory).
 char* host_stage(sphg_sim* s, size_t bytes);
+// In-cell offset o (FP64, in [0, cs)) as FP32, kept below cs after rounding.
+float split_offset(double o, double cs);
 // Instance holding particle i (instances are contiguous in particle order).
 int instance_of(const sphg_sim* s, int64_t i);
 uint32_t morton_host(uint32_t x, uint32_t y);

@@ -16,8 +16,8 @@
 // same decision word and skip themselves otherwise).
 //
 // Kernels: movers_compact (mover list in slot order, movers before each word,
-// decision), movers_sort_place (bitonic sort of the movers in shared memory,
-// their final positions), stayers_place (every stayer's final position).
+// decision), movers_sort (bitonic sort of the movers in shared memory),
+// movers_merge (final position of every stayer and every mover).
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -111,27 +111,19 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
   }
 }
 
-// lower bound of (key, slot) among the slots' (keyA[s], s): slots are sorted by it
+// Number of slots s with (keyA[s], s) < (k, sl): the slots are in that order.
 __device__ __forceinline__ int64_t slots_before(const MoverArgs& a, uint32_t k, uint32_t sl) {
   int64_t lo = 0, hi = a.n;
-  while (lo < hi) {  // first slot with keyA >= k
+  while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
-    if (a.keyA[mid] < k) lo = mid + 1;
+    const uint32_t km = a.keyA[mid];
+    if (km < k || (km == k && mid < (int64_t)sl)) lo = mid + 1;
     else hi = mid;
   }
-  const int64_t first = lo;
-  hi = a.n;
-  while (lo < hi) {  // first slot with keyA > k
-    const int64_t mid = (lo + hi) >> 1;
-    if (a.keyA[mid] <= k) lo = mid + 1;
-    else hi = mid;
-  }
-  const int64_t last = lo;
-  const int64_t s = (int64_t)sl;
-  return s < first ? first : (s > last ? last : s);
+  return lo;
 }
 
-__global__ void __launch_bounds__(kPlaceThreads) movers_sort_place(MoverArgs a) {
+__global__ void __launch_bounds__(kPlaceThreads) movers_sort(MoverArgs a) {
   extern __shared__ unsigned long long sm[];
   if (!a.ctl[0]) return;
   const uint32_t m = a.ctl[1];
@@ -157,29 +149,31 @@ __global__ void __launch_bounds__(kPlaceThreads) movers_sort_place(MoverArgs a) 
       __syncthreads();
     }
   }
-  for (uint32_t r = threadIdx.x; r < m; r += blockDim.x) {
-    const unsigned long long v = sm[r];
-    const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
-    a.msorted[r] = v;
-    const int64_t p = slots_before(a, k, sl);
-    const int64_t fin = (int64_t)r + (p - (int64_t)movers_before(a, p, m));
-    a.keyS[fin] = k;
-    a.perm[fin] = sl;
-  }
+  for (uint32_t r = threadIdx.x; r < m; r += blockDim.x) a.msorted[r] = sm[r];
 }
 
-__global__ void __launch_bounds__(kStayThreads) stayers_place(MoverArgs a) {
+// Thread i places slot i if it kept its key, and the i-th smallest mover.
+__global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   if (!a.ctl[0]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  if ((a.mask[i >> 5] >> (i & 31)) & 1u) return;
   const uint32_t m = a.ctl[1];
+  if (i < (int64_t)m) {  // a mover: its rank among movers + the stayers ordered before it
+    const unsigned long long v = a.msorted[i];
+    const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
+    const int64_t p = slots_before(a, k, sl);
+    const int64_t fin = i + (p - (int64_t)movers_before(a, p, m));
+    a.keyS[fin] = k;
+    a.perm[fin] = sl;
+  }
+  if ((a.mask[i >> 5] >> (i & 31)) & 1u) return;
+  // a stayer: its rank among stayers + the movers ordered before it
   const uint32_t k = a.keyA[i];
   const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
-  uint32_t lo = 0, hi = m;  // movers ordered before this stayer
+  uint32_t lo = 0, hi = m;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
-    if ((unsigned long long)a.msorted[mid] < v) lo = mid + 1;
+    if (a.msorted[mid] < v) lo = mid + 1;
     else hi = mid;
   }
   const int64_t fin = i - (int64_t)movers_before(a, i, m) + lo;
@@ -195,14 +189,14 @@ cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(movers_sort_place, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(movers_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kMoverCap * (int)sizeof(unsigned long long));
     if (e != cudaSuccess) return e;
     attr = true;
   }
   movers_compact<<<mover_groups(a.n), kCompactThreads, 0, st>>>(a);
-  movers_sort_place<<<1, kPlaceThreads, kMoverCap * sizeof(unsigned long long), st>>>(a);
-  stayers_place<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
+  movers_sort<<<1, kPlaceThreads, kMoverCap * sizeof(unsigned long long), st>>>(a);
+  movers_merge<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

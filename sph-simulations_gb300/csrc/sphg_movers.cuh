@@ -24,7 +24,7 @@ struct MoverArgs {
 };
 
 int mover_groups(int64_t n);
-// movers_compact, movers_sort_place, stayers_place; when more than kMoverCap
+// movers_compact, movers_sort, movers_merge; when more than kMoverCap
 // slots changed they do nothing and leave ctl[0] = 0 for the full sort.
 cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st);
 

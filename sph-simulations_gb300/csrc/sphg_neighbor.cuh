@@ -22,7 +22,17 @@ __device__ __forceinline__ InstDesc inst_of(const StepArgs& a, int64_t i) {
 }
 
 static __device__ __noinline__ int offset_cells_d(float o, double cs_d) {
-  return offset_cells_d(o, cs_d);
+  return (int)floor(__ddiv_rn((double)o, cs_d));
+}
+
+// Offset o moved k cells: o - k cs in FP64, rounded to FP32 and kept inside
+// [0, cs) of the FP64 cell size (a rounding up to cs is stepped back one ulp),
+// so the reconstructed position lo + c cs + o stays in cell c.  Out of line:
+// runs only for particles that changed cell.
+static __device__ __noinline__ float offset_shift_d(float o, int k, double cs_d) {
+  float r = __double2float_rn(__dsub_rn((double)o, (double)k * cs_d));
+  if ((double)r >= cs_d) r = nextafterf(r, 0.0f);
+  return r;
 }
 
 // floor(o / cs) for a split-precision offset, FP64 near integer boundaries.
@@ -274,17 +284,20 @@ __device__ __forceinline__ uint32_t integrate_and_key(const StepArgs& a, const I
     const int ky = offset_cells(y, d.inv_cs_y, d.cs_yd);
     nx_ = cx + kx;
     ny_ = cy + ky;
+    int sx, sy;  // cells the offset moves by
     if (d.periodic) {
-      x -= (float)kx * d.cs_x;
-      y -= (float)ky * d.cs_y;
+      sx = kx;
+      sy = ky;
       nx_ = ((nx_ % d.nxr) + d.nxr) % d.nxr;
       ny_ = ((ny_ % d.nyr) + d.nyr) % d.nyr;
     } else {
       nx_ = nx_ < 0 ? 0 : (nx_ > cmx ? cmx : nx_);
       ny_ = ny_ < 0 ? 0 : (ny_ > cmy ? cmy : ny_);
-      x -= (float)(nx_ - cx) * d.cs_x;
-      y -= (float)(ny_ - cy) * d.cs_y;
+      sx = nx_ - cx;
+      sy = ny_ - cy;
     }
+    if (sx) x = offset_shift_d(x, sx, d.cs_xd);
+    if (sy) y = offset_shift_d(y, sy, d.cs_yd);
   }
   const uint32_t key = d.cell_base + local_code(d, nx_, ny_);
   a.posB[i] = make_float2(x, y);

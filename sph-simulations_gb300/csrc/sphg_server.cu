@@ -129,7 +129,8 @@ void stage_newcomer(sphg_server* s, const SrvReq& r, const InstDesc& d, size_t a
     if (sim->opt.precision == SPHG_PRECISION_SPLIT) {
       cx = host_cell(r.x[i], d.lo_xd, d.cs_xd, cmx);
       cy = host_cell(r.y[i], d.lo_yd, d.cs_yd, cmy);
-      pos = make_float2((float)((r.x[i] - d.lo_xd) - cx * d.cs_xd), (float)((r.y[i] - d.lo_yd) - cy * d.cs_yd));
+      pos = make_float2(split_offset((r.x[i] - d.lo_xd) - cx * d.cs_xd, d.cs_xd),
+                        split_offset((r.y[i] - d.lo_yd) - cy * d.cs_yd, d.cs_yd));
     } else {
       const float fx = (float)r.x[i], fy = (float)r.y[i];
       cx = host_cell((double)fx, d.lo_xd, d.cs_xd, cmx);

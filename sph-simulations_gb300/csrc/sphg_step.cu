@@ -53,17 +53,18 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
       int ky = offset_cells(p.y, d.inv_cs_y, d.cs_yd);
       cx = ox + kx;
       cy = oy + ky;
+      int sx = kx, sy = ky;  // cells the offset moves by
       if (d.periodic) {
-        p.x -= (float)kx * d.cs_x;
-        p.y -= (float)ky * d.cs_y;
         cx = ((cx % d.nxr) + d.nxr) % d.nxr;
         cy = ((cy % d.nyr) + d.nyr) % d.nyr;
       } else {
         cx = cx < 0 ? 0 : (cx > cmx ? cmx : cx);
         cy = cy < 0 ? 0 : (cy > cmy ? cmy : cy);
-        p.x -= (float)(cx - ox) * d.cs_x;
-        p.y -= (float)(cy - oy) * d.cs_y;
+        sx = cx - ox;
+        sy = cy - oy;
       }
+      if (sx) p.x = offset_shift_d(p.x, sx, d.cs_xd);
+      if (sy) p.y = offset_shift_d(p.y, sy, d.cs_yd);
       a.posB[i] = p;
     }
     key = d.cell_base + local_code(d, cx, cy);
@@ -189,24 +190,24 @@ template <int PREC, bool BATCHED, int MODE, bool CSR>
 __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
   __shared__ float2 bd[kForceBuf][kThreads];
   __shared__ uint32_t bj[kForceBuf][kThreads];
-  __shared__ uint32_t hs[4][256];
-  const bool hist = (MODE == kForceIntegrate) && a.ghist != nullptr;
-  if (hist) {
-    for (int p = 0; p < 4; ++p) hs[p][threadIdx.x] = 0;
-    __syncthreads();
-  }
+  __shared__ uint32_t moved_in_block;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
+  const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
+  if (track && threadIdx.x == 0) moved_in_block = 0;
   uint32_t key = 0;
   if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, bd, bj);
-  if (hist) histogram_keys(a, hs, valid, key);
-  if (MODE == kForceIntegrate && a.mover_mask) {
-    // slots whose cell key changed, for the incremental re-sort (a warp holds 32 consecutive slots)
+  if (track) {
+    // slots whose cell key changed, for the incremental re-sort: one bit per
+    // slot (a warp holds 32 consecutive slots), one count per block
     const unsigned moved = __ballot_sync(0xffffffffu, valid && key != a.keyA[i]);
     if ((threadIdx.x & 31) == 0 && valid) {
       a.mover_mask[i >> 5] = moved;
-      if (moved) atomicAdd(a.mover_gsum + (i >> 16), (uint32_t)__popc(moved));
+      if (moved) atomicAdd(&moved_in_block, (uint32_t)__popc(moved));
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && moved_in_block)
+      atomicAdd(a.mover_gsum + (((int64_t)blockIdx.x * blockDim.x) >> 16), moved_in_block);
   }
 }
 

@@ -18,7 +18,7 @@ OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY, NOT_READY = rang
 ORDER = {"morton": 0, "rowmajor": 1}
 PLAIN, SPLIT = 0, 1
 SORTED, LISTS = 0, 1
-DBG_KEYS, DBG_PERM, DBG_UNSORTED_KEYS, DBG_POS_NEXT, DBG_VEL_NEXT = range(5)
+DBG_KEYS, DBG_PERM, DBG_UNSORTED_KEYS, DBG_POS_NEXT, DBG_VEL_NEXT, DBG_RESORT = range(6)
 
 
 class SphgError(RuntimeError):
@@ -214,6 +214,8 @@ class Sim:
     def debug(self, which, stream=None):
         if which in (DBG_POS_NEXT, DBG_VEL_NEXT):
             out = np.empty(2 * self.n, np.float64)
+        elif which == DBG_RESORT:
+            out = np.zeros(2, np.int32)
         else:
             out = np.empty(self.n, np.int32)
         check(lib().sphg_get_debug(self._h, which, out.ctypes.data_as(_vp), _stream(stream)))

@@ -684,7 +684,8 @@ def test_encoded_lists_round_trip(golden):
 def test_incremental_resort_equals_full_sort_bitwise(prec, vel):
     """resort=1 merges the particles that changed cell into the rest; it must give
     the full radix sort's order and therefore the same bits.  vel=400 moves more
-    than 8,192 particles a step, so the device falls back to the full sort."""
+    than 8,192 particles in the first iterations, so the device falls back to the
+    full sort there (and merges again once the particles pile up at the walls)."""
     S = _sphg()
     P = S.SPLIT if prec == "split" else S.PLAIN
     x, y, vx, vy = jittered(160, 120, 0.005, seed=31, vel=vel)
@@ -709,6 +710,6 @@ def test_incremental_resort_equals_full_sort_bitwise(prec, vel):
     if vel < 1:
         assert 0 < max(moved) <= 8192
     else:
-        assert min(moved) > 8192
+        assert max(moved) > 8192  # at least one iteration took the full sort
     for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids", "keys", "perm"):
         assert np.array_equal(a[f], b[f], equal_nan=True), f

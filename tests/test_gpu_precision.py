@@ -1,0 +1,82 @@
+"""Error of the CUDA path against the FP64 oracle on the 1,000,000-particle dam
+break (1000 x 1000 particles, dx = 0.0005, h = 1.3 dx, alpha = 0.1, g = -9.81,
+rho0 = 1000, dt = 1e-5) after 1 and 100 main-loop iterations, in both
+precision modes:
+  * density and acceleration per step: the oracle evaluated on the GPU's own
+    state of that step (max per-particle |drho|/rho; max |da| / max |a|);
+  * positions, free-running: the GPU run against the oracle run from the same
+    initial state, particles matched by creation index, max |dx| in units of
+    the lattice spacing.
+The figures are printed as one PRECISION_REPORT line (pytest -s)."""
+import json
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RHO_TOL = 1e-5
+ACC_TOL = 1e-5
+
+
+def _errors(p, g, keys):
+    """Oracle density/forces on the GPU state with the GPU's cell keys (in split
+    precision the key is part of the position; the FP64 reconstruction
+    lo + c cs + o can round across a cell edge)."""
+    sk = keys
+    s, e = O.cell_ranges(p, sk)
+    rho = O.density(p, g["x"], g["y"], sk, s, e)
+    fx, fy = O.forces(p, g["x"], g["y"], g["vx"], g["vy"], rho, sk, s, e)
+    drho = float(np.max(np.abs(g["rho"] - rho) / rho))
+    scale = max(np.abs(fx).max(), np.abs(fy).max())
+    dacc = float(max(np.abs(g["fx"] - fx).max(), np.abs(g["fy"] - fy).max()) / scale)
+    return drho, dacc
+
+
+def test_precision_report_1m_dam_break():
+    import sphg as S
+    import workloads as W
+    prm, x, y, vx, vy = W.dam_break(1000, 1000, 0.0005, seed=0)
+    dx = 0.0005
+    p = O.params(**prm)
+    ref = O.Sim(p, x, y, vx, vy)
+    ref.preloop()
+    report = {"workload": "dam_break_1m", "particles": len(x)}
+    sims = {m: S.Sim(S.params(**prm), len(x), S.options(precision=P)) for m, P in
+            (("plain", S.PLAIN), ("split", S.SPLIT))}
+    for sim in sims.values():
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+    done = 0
+    for k in (1, 100):
+        ref.steps(k - done)
+        r = ref.get()
+        rpos = np.empty((len(x), 2))
+        rpos[r["ids"]] = np.stack([r["x"], r["y"]], 1)
+        for mode, sim in sims.items():
+            sim.step(k - done)
+            g = sim.download()
+            keys = sim.debug(S.DBG_KEYS)
+            recomputed = O.cell_ids(p, g["x"], g["y"])
+            off = np.nonzero(recomputed != keys)[0]
+            if mode == "plain":
+                assert len(off) == 0
+            else:  # only reconstructions that land within rounding of a cell edge
+                cs = prm["h"]
+                for q in off[:50]:
+                    fx_ = (g["x"][q] - prm["lo"][0]) / cs
+                    fy_ = (g["y"][q] - prm["lo"][1]) / cs
+                    edge = min(abs(fx_ - round(fx_)), abs(fy_ - round(fy_)))
+                    assert edge < 1e-9, (mode, k, q, g["x"][q], g["y"][q])
+            drho, dacc = _errors(p, g, keys)
+            dpos = float(np.max(np.hypot(g["x"] - rpos[g["ids"], 0], g["y"] - rpos[g["ids"], 1])) / dx)
+            report["%s_step%d" % (mode, k)] = {"density_rel": drho, "accel_rel": dacc, "pos_over_dx": dpos,
+                                               "cells_at_rounding_edge": int(len(off))}
+            assert drho <= RHO_TOL and dacc <= ACC_TOL, (mode, k, drho, dacc)
+            assert dpos < 1e-3, (mode, k, dpos)
+        done = k
+    for sim in sims.values():
+        sim.close()
+    print("PRECISION_REPORT " + json.dumps(report))
