@@ -181,6 +181,10 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 // times instead of once per candidate iteration.  A thread with more than
 // kForceBuf neighbours handles the extra ones inline during the scan.
 constexpr int kForceBuf = 12;
+#ifndef SPHG_FORCE_BATCH
+#define SPHG_FORCE_BATCH 4
+#endif
+constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered together
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
@@ -225,9 +229,8 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
   const float alpha_c0 = d.alpha_c0;
   const float4* __restrict__ velp = a.velpA;
-  auto pair = [&](uint32_t j, float dx, float dy) {
+  auto pair_v = [&](const float4 vj, float dx, float dy) {
     const float r2 = fmaf(dx, dx, dy * dy);
-    const float4 vj = __ldg(velp + j);
     const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
     const float r = r2 * rinv;
     const float hr = h - r;
@@ -251,6 +254,7 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
       }
     }
   };
+  auto pair = [&](uint32_t j, float dx, float dy) { pair_v(__ldg(velp + j), dx, dy); };
   int cx, cy;
   const uint32_t cnt = CSR ? 0u : (a.nbr ? a.ncount[i] : 0xffffffffu);
   if (CSR) {
@@ -270,7 +274,27 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
     // the density pass recorded this particle's neighbours (stencil order)
     decode_code(d, key - d.cell_base, cx, cy);
     const size_t n = (size_t)a.n;
-    for (uint32_t q = 0; q < cnt; ++q) {
+    uint32_t q = 0;
+    // kForceBatch neighbours at a time: their gathers are in flight together
+    for (; q + kForceBatch <= cnt; q += kForceBatch) {
+      uint32_t e[kForceBatch];
+      float2 pj[kForceBatch];
+      float4 vj[kForceBatch];
+#pragma unroll
+      for (int u = 0; u < kForceBatch; ++u) e[u] = __ldg(a.nbr + (q + u) * n + i);
+#pragma unroll
+      for (int u = 0; u < kForceBatch; ++u) {
+        pj[u] = __ldg(a.posA + (e[u] >> 5));
+        vj[u] = __ldg(velp + (e[u] >> 5));
+      }
+#pragma unroll
+      for (int u = 0; u < kForceBatch; ++u) {
+        float dx, dy;
+        entry_vec<PREC>(d, pi, pj[u], e[u], dx, dy);
+        pair_v(vj[u], dx, dy);
+      }
+    }
+    for (; q < cnt; ++q) {
       const uint32_t e = __ldg(a.nbr + q * n + i);
       float dx, dy;
       entry_vec<PREC>(d, pi, __ldg(a.posA + (e >> 5)), e, dx, dy);
