@@ -250,14 +250,19 @@ def run_gpu(args):
     phases, resort = [], []
     for _ in range(20):
         phases.append(sim.profile_step(stream=sptr))
-        resort.append(sim.debug(sphg.DBG_RESORT, stream=sptr).tolist())
+        resort.append(sim.debug(sphg.DBG_RESORT, stream=sptr)[:2].tolist())
     phases = np.array(phases)
     phase_ms = phases.mean(axis=0).tolist()
     resort = np.array(resort)
     resort_out = {"incremental_fraction": float(resort[:, 0].mean()),
                   "cell_changes_per_step": float(resort[:, 1].mean())}
     diag = sim.diagnostics(stream=sptr)
-    launches = sim.launches_per_step() * args.steps
+    # kernels per timed iteration: the full sort's histogram + radix passes run only
+    # on iterations that did not merge (they sit under a conditional graph node)
+    full_sort_kernels = int(sim.debug(sphg.DBG_RESORT, stream=sptr)[2])
+    per_step = sim.launches_per_step()
+    merged = resort_out["incremental_fraction"]
+    launches = int(round(args.steps * (per_step - merged * full_sort_kernels)))
     sim.close()
 
     extra = {}

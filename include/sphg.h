@@ -139,6 +139,15 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
  * sum m vx, sum m vy, non-finite count.  out has 6*ninst entries. */
 sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream);
 
+/* Adaptive time step per instance from the current state: FP64 maxima of the
+ * speed and of the acceleration on the device, then
+ *   dt = min(cfl * h / (c0 + max|v|), force_coef * sqrt(h / max|a|))
+ * (infinite when both are zero).  out has ninst entries.  The reference steps
+ * with a fixed dt (config/example.txt); apply a new one with sphg_set_dt. */
+sphg_status sphg_cfl_dt(sphg_sim* s, double cfl, double force_coef, double* out, void* stream);
+/* Time step of instance inst (every instance when inst < 0) from the next iteration on. */
+sphg_status sphg_set_dt(sphg_sim* s, int32_t inst, double dt);
+
 /* Debug / parity views (host copies, current slot order).  which: */
 enum {
   SPHG_DBG_KEYS = 0,        /* int32[n]  sorted cell keys (instance-local codes) */
@@ -146,8 +155,9 @@ enum {
   SPHG_DBG_UNSORTED_KEYS = 2,/* int32[n] keys of the integrated state awaiting the next sort */
   SPHG_DBG_POS_NEXT = 3,    /* double[2n] integrated positions awaiting the next sort */
   SPHG_DBG_VEL_NEXT = 4,    /* double[2n] integrated velocities awaiting the next sort */
-  SPHG_DBG_RESORT = 5       /* int32[2]  last iteration: 1 if the incremental re-sort ran
-                               (0: the full radix sort), particles that changed cell */
+  SPHG_DBG_RESORT = 5       /* int32[3]  last iteration: 1 if the incremental re-sort ran
+                               (0: the full radix sort), particles that changed cell,
+                               kernels of a full sort (histogram + radix passes) */
 };
 sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream);
 
@@ -205,11 +215,25 @@ sphg_status sphg_server_result(sphg_server* s, int64_t request_id, double* x, do
  * capacity (cell keys), live particles. */
 sphg_status sphg_server_stats(sphg_server* s, double* out);
 
+/* Autotuner: times every candidate launch configuration of this workload (the
+ * cell-block shape: one thread per particle or Morton cell tiles of 2^b x 2^b
+ * cells, b = 3..5; the re-sort strategy: incremental merge or full radix sort)
+ * on handles of its own with the given state (pre-loop, 3 warm-up and `steps`
+ * timed main-loop iterations on `stream`), and returns the fastest in *best
+ * (precision, track_ids, use_graph and compute as in *base) with its
+ * milliseconds per iteration.  Results are remembered per workload for the
+ * process.  No reference counterpart (its block size is a config key,
+ * gpu_threads_per_block, config/example.txt). */
+sphg_status sphg_autotune(int32_t ninst, const sphg_params* p, const int64_t* counts, const double* x,
+                          const double* y, const double* vx, const double* vy, const sphg_options* base,
+                          int32_t steps, sphg_options* best, double* ms_per_step, void* stream);
+
 /* Runs one main-loop iteration kernel by kernel with CUDA events between the
  * phases; ms[0..4] = keys, sort, reorder (+cell ranges), density, force+integrate
  * (milliseconds, summed over the instances of the handle). */
 sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream);
-/* Number of kernel launches one main-loop iteration makes. */
+/* Kernel launches of a main-loop iteration that runs the full sort; in a graph,
+ * an iteration that merges launches SPHG_DBG_RESORT[2] fewer. */
 int32_t sphg_launches_per_step(const sphg_sim* s);
 
 /* Stand-alone kernels on caller-owned DEVICE buffers. */

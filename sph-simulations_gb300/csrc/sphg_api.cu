@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <thread>
 #include <vector>
@@ -220,40 +221,42 @@ void set_last_error(const std::string& msg) { sphg_detail::g_err = msg; }
 
 namespace sphg_detail {
 
-// One main-loop iteration.  The force kernel writes the keys of the integrated
-// state, so the key pass only runs on the first iteration after an upload.
-// With ev (6 events) the phase boundaries are recorded: start, keys, sort,
-// reorder, density, force.
-sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* ev) {
+// The incremental re-sort's kernels (see sphg_movers.cu).  cond, when not 0,
+// is the graph's conditional handle that guards the full sort: the decision
+// kernel sets it to 0 when the merge handled the iteration.
+sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond) {
+  sphg::MoverArgs m;
+  m.n = s->n;
+  m.keyA = s->keyA;
+  m.keyB = s->keyB;
+  m.mask = s->mmask;
+  m.gsum = s->mgsum;
+  m.wprefix = s->mwprefix;
+  m.movers = s->mlist;
+  m.msorted = s->msorted;
+  m.ctl = s->flags + 3;
+  m.epoch = s->flags + 2;
+  m.keyS = s->keyTmp;
+  m.perm = s->perm;
+  m.cond = cond;
+  SPHG_CUDA(sphg::launch_movers(m, st));
+  return SPHG_OK;
+}
+
+// The full stable radix sort of the next keys (skip: device word that makes
+// its kernels return at once, or null).
+sphg_status enqueue_full_sort(sphg_sim* s, cudaStream_t st, const uint32_t* skip) {
+  const StepArgs a = s->args();
+  SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyTmp, s->perm, s->keyA, s->valTmp,
+                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist, skip));
+  if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
+  return SPHG_OK;
+}
+
+// Reorder + cell ranges, density, forces + integration (ev: events 3..5).
+sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
-  if (ev) SPHG_CUDA(cudaEventRecord(ev[0], st));
-  if (first) SPHG_CUDA(sphg::launch_keys(a, prec, st));
-  if (ev) SPHG_CUDA(cudaEventRecord(ev[1], st));
-  // the force pass of the previous iteration recorded which slots changed
-  // cell: merge them in when few did (the full sort's kernels then skip)
-  const bool inc = s->movers_on && !first;
-  if (inc) {
-    sphg::MoverArgs m;
-    m.n = s->n;
-    m.keyA = s->keyA;
-    m.keyB = s->keyB;
-    m.mask = s->mmask;
-    m.gsum = s->mgsum;
-    m.wprefix = s->mwprefix;
-    m.movers = s->mlist;
-    m.msorted = s->msorted;
-    m.ctl = s->flags + 3;
-    m.epoch = s->flags + 2;
-    m.keyS = s->keyTmp;
-    m.perm = s->perm;
-    SPHG_CUDA(sphg::launch_movers(m, st));
-  }
-  SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyTmp, s->perm, s->keyA, s->valTmp,
-                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist,
-                                   inc ? s->flags + 3 : nullptr));
-  if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
-  if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[3], st));
@@ -292,9 +295,98 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
   return SPHG_OK;
 }
 
+// One main-loop iteration.  The force kernel writes the keys of the integrated
+// state, so the key pass only runs on the first iteration after an upload.
+// With ev (6 events) the phase boundaries are recorded: start, keys, sort,
+// reorder, density, force.
+sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* ev) {
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[0], st));
+  if (first) SPHG_CUDA(sphg::launch_keys(s->args(), s->opt.precision, st));
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[1], st));
+  // the force pass of the previous iteration recorded which slots changed
+  // cell: merge them in when few did (the full sort's kernels then skip)
+  const bool inc = s->movers_on && !first;
+  if (inc) SPHG_TRY(enqueue_movers(s, st, 0));
+  SPHG_TRY(enqueue_full_sort(s, st, inc ? s->flags + 3 : nullptr));
+  if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));
+  return enqueue_after_sort(s, st, ev);
+}
+
+// Graph of one iteration with the full sort under a conditional node: the
+// incremental re-sort's decision kernel switches it off, so iterations that
+// merge launch none of the full sort's kernels.
+sphg_status build_graph_conditional(sphg_sim* s) {
+  if (!s->cap_stream2) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream2, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  SPHG_CUDA(cudaGraphCreate(&g, 0));
+  auto done = [&](sphg_status st) {
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(s->cap_stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(s->cap_stream, &junk);
+      if (junk && junk != g) cudaGraphDestroy(junk);
+    }
+    if (cudaStreamIsCapturing(s->cap_stream2, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(s->cap_stream2, &junk);
+    }
+    if (g) cudaGraphDestroy(g);
+    return st;
+  };
+  cudaGraphConditionalHandle h = 0;
+  if (cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault) != cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "conditional handle"));
+  if (cudaStreamBeginCaptureToGraph(s->cap_stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "capture to graph"));
+  sphg_status st = enqueue_movers(s, s->cap_stream, (unsigned long long)h);
+  if (st != SPHG_OK) return done(st);
+  cudaStreamCaptureStatus cst;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  if (cudaStreamGetCaptureInfo(s->cap_stream, &cst, nullptr, nullptr, &deps, nullptr, &ndeps) != cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "capture info"));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode = nullptr;
+  if (cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp) != cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "conditional node"));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(s->cap_stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "capture of the conditional body"));
+  st = enqueue_full_sort(s, s->cap_stream2, nullptr);
+  cudaGraph_t body_out = nullptr;
+  const cudaError_t eb = cudaStreamEndCapture(s->cap_stream2, &body_out);
+  if (st != SPHG_OK) return done(st);
+  if (eb != cudaSuccess) return done(fail(SPHG_CUDA_ERROR, "end of the conditional body capture"));
+  if (cudaStreamUpdateCaptureDependencies(s->cap_stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+    return done(fail(SPHG_CUDA_ERROR, "capture dependencies"));
+  st = enqueue_after_sort(s, s->cap_stream, nullptr);
+  if (st != SPHG_OK) return done(st);
+  cudaGraph_t out = nullptr;
+  if (cudaStreamEndCapture(s->cap_stream, &out) != cudaSuccess) return done(fail(SPHG_CUDA_ERROR, "end capture"));
+  const cudaError_t e = cudaGraphInstantiate(&s->gexec, g, 0);
+  cudaGraphDestroy(g);
+  g = nullptr;
+  if (e != cudaSuccess) {
+    s->gexec = nullptr;
+    return fail(SPHG_CUDA_ERROR, std::string("instantiate: ") + cudaGetErrorString(e));
+  }
+  return SPHG_OK;
+}
+
 sphg_status build_graph(sphg_sim* s) {
   if (s->gexec) return SPHG_OK;
   if (!s->cap_stream) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+  if (s->movers_on && s->cond_graph) {
+    if (build_graph_conditional(s) == SPHG_OK) return SPHG_OK;
+    s->cond_graph = false;  // not available here: the full sort's kernels skip themselves instead
+    cudaGetLastError();
+  }
   cudaGraph_t g = nullptr;
   SPHG_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
   sphg_status st = enqueue_step(s, s->cap_stream);
@@ -485,6 +577,7 @@ sphg_status destroy_impl(sphg_sim* s) {
   if (!s) return SPHG_OK;
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  if (s->cap_stream2) cudaStreamDestroy(s->cap_stream2);
   if (s->arena.base) cudaFree(s->arena.base);
   if (s->csr_idx) cudaFree(s->csr_idx);
   if (s->hstage) cudaFreeHost(s->hstage);
@@ -714,6 +807,49 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream) {
   return SPHG_OK;
 }
 
+sphg_status sphg_cfl_dt(sphg_sim* s, double cfl, double force_coef, double* out, void* stream) {
+  if (!s || !out || !(cfl > 0) || !(force_coef > 0)) return fail(SPHG_INVALID_ARG, "null argument or coefficient <= 0");
+  if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->n > 0) {
+    SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
+    int64_t max_n = 0;
+    for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
+    const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
+    SPHG_CUDA(sphg::launch_cfl(s->args(), s->diag_partials, chunks, s->diag_out, st));
+  }
+  std::vector<double> m((size_t)6 * s->ninst, 0.0);
+  if (s->n > 0) {
+    SPHG_CUDA(cudaMemcpyAsync(m.data(), s->diag_out, sizeof(double) * 6 * s->ninst, cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+  }
+  for (int i = 0; i < s->ninst; ++i) {
+    const sphg_params& p = s->params[i];
+    const double vmax = std::sqrt(m[6 * i]), amax = std::sqrt(m[6 * i + 1]);
+    double dt = std::numeric_limits<double>::infinity();
+    if (p.c0 + vmax > 0) dt = std::min(dt, cfl * p.h / (p.c0 + vmax));
+    if (amax > 0) dt = std::min(dt, force_coef * std::sqrt(p.h / amax));
+    out[i] = dt;
+  }
+  return SPHG_OK;
+}
+
+sphg_status sphg_set_dt(sphg_sim* s, int32_t inst, double dt) {
+  if (!s || !(dt > 0) || !std::isfinite(dt) || inst >= s->ninst) return fail(SPHG_INVALID_ARG, "bad handle, instance or dt");
+  const int b = inst < 0 ? 0 : inst, e = inst < 0 ? s->ninst : inst + 1;
+  for (int i = b; i < e; ++i) {
+    s->params[i].dt = dt;
+    s->hdesc[i].dt = (float)dt;
+  }
+  if (s->ninst > 0)
+    SPHG_CUDA(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * s->ninst, cudaMemcpyHostToDevice));
+  if (s->gexec) {  // the single-instance descriptor is a kernel argument of the captured graph
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+  }
+  return SPHG_OK;
+}
+
 sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream) {
   if (!s || !host) return fail(SPHG_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
@@ -732,11 +868,12 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
   };
   switch (which) {
     case SPHG_DBG_RESORT: {
-      uint32_t c[2] = {0, 0};
+      uint32_t c[3] = {0, 0, 0};
       if (s->movers_on) {
-        SPHG_CUDA(cudaMemcpyAsync(c, s->flags + 3, sizeof(c), cudaMemcpyDeviceToHost, st));
+        SPHG_CUDA(cudaMemcpyAsync(c, s->flags + 3, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         SPHG_CUDA(cudaStreamSynchronize(st));
       }
+      c[2] = (uint32_t)((s->key_bits + 7) / 8 + 1);  // histogram + radix passes of a full sort
       std::memcpy(host, c, sizeof(c));
       return SPHG_OK;
     }
@@ -908,9 +1045,10 @@ sphg_status sphg_profile_step(sphg_sim* s, float* ms, void* stream) {
 int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
-  // the sort's histogram kernel + radix passes + reorder + density + force
-  // (+ the three incremental re-sort kernels; + list count, three scan kernels
-  // and list fill in the lists mode)
+  // an iteration that runs the full sort: its histogram kernel + radix passes +
+  // reorder + density + force (+ the three incremental re-sort kernels; + list
+  // count, three scan kernels and list fill in the lists mode).  An iteration
+  // that merges launches (key_bits + 7) / 8 + 1 kernels fewer in a graph.
   return passes + 4 + (s->movers_on ? 3 : 0) + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
 }
 

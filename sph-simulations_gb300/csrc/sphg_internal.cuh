@@ -79,7 +79,8 @@ struct sphg_sim {
   char* hstage = nullptr;
   size_t hstage_bytes = 0;
   // CUDA graph of one step
-  cudaStream_t cap_stream = nullptr;
+  cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;
+  bool cond_graph = true;       // full sort under a conditional graph node (when the merge is on)
   cudaGraphExec_t gexec = nullptr;
 
   StepArgs args() const {

@@ -7,16 +7,16 @@
 // is then a merge of two sorted sequences:
 //   * stayers: slots whose key did not change -- already in (key, slot) order,
 //     because the current state is sorted;
-//   * movers: slots whose key changed -- few, sorted here in one CTA.
+//   * movers: slots whose key changed -- few, ranked here by counting.
 // A stayer's new position is its rank among stayers plus the number of movers
 // ordered before it; a mover's is its rank among movers plus the number of
 // stayers ordered before it.  The force pass records which slots moved (one
-// bit per slot, and a count per group of 65,536 slots); when more than
+// bit per slot, and a count per group of 8,192 slots); when more than
 // kMoverCap slots moved, the full radix sort runs instead (its kernels read the
 // same decision word and skip themselves otherwise).
 //
 // Kernels: movers_compact (mover list in slot order, movers before each word,
-// decision), movers_sort (bitonic sort of the movers in shared memory),
+// decision), movers_rank (each mover's rank by counting the smaller ones),
 // movers_merge (final position of every stayer and every mover).
 #include <cstdint>
 
@@ -29,8 +29,9 @@ namespace sphg {
 namespace {
 
 constexpr int kCompactThreads = 256;
-constexpr int kCompactWords = 8;  // words per thread: 256 x 8 words = one group of 65,536 slots
-constexpr int kPlaceThreads = 1024;
+constexpr int kCompactWords = 1;  // words per thread: 256 x 1 word = one group of 8,192 slots
+static_assert(kCompactThreads * kCompactWords * 32 == (1 << kGroupShift), "one block per group");
+constexpr int kRankTile = 128;
 constexpr int kStayThreads = 256;
 
 __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p, uint32_t m) {
@@ -71,6 +72,7 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
     a.ctl[0] = inc ? 1u : 0u;
     a.ctl[1] = tot;
     if (inc) *a.epoch += 1u;  // the step epoch the skipped radix sort would have bumped
+    if (a.cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, inc ? 0u : 1u);
   }
   if (!inc) return;
   const int64_t nwords = (a.n + 31) >> 5;
@@ -123,40 +125,32 @@ __device__ __forceinline__ int64_t slots_before(const MoverArgs& a, uint32_t k, 
   return lo;
 }
 
-__global__ void __launch_bounds__(kPlaceThreads) movers_sort(MoverArgs a) {
+// Rank of each mover among the movers = how many (key, slot) pairs are smaller
+// (all distinct); the mover list is staged in shared memory once per CTA and
+// every thread counts against all of it.  kRankTile movers per CTA; CTAs past
+// the mover count exit.
+__global__ void __launch_bounds__(kRankTile) movers_rank(MoverArgs a) {
   extern __shared__ unsigned long long sm[];
   if (!a.ctl[0]) return;
   const uint32_t m = a.ctl[1];
-  if (m == 0) return;
-  uint32_t cap = 2;
-  while (cap < m) cap <<= 1;
-  for (uint32_t r = threadIdx.x; r < cap; r += blockDim.x)
-    sm[r] = r < m ? (unsigned long long)a.movers[r] : ~0ull;
+  const uint32_t r = blockIdx.x * kRankTile + threadIdx.x;
+  if (blockIdx.x * kRankTile >= m) return;
+  for (uint32_t q = threadIdx.x; q < m; q += blockDim.x) sm[q] = a.movers[q];
   __syncthreads();
-  // bitonic sort, ascending on (key << 32 | slot)
-  for (uint32_t k = 2; k <= cap; k <<= 1) {
-    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-      for (uint32_t t = threadIdx.x; t < (cap >> 1); t += blockDim.x) {
-        const uint32_t i0 = 2 * t - (t & (j - 1));  // lower index of the pair
-        const uint32_t i1 = i0 + j;
-        const bool up = (i0 & k) == 0;
-        const unsigned long long u = sm[i0], v = sm[i1];
-        if ((u > v) == up) {
-          sm[i0] = v;
-          sm[i1] = u;
-        }
-      }
-      __syncthreads();
-    }
-  }
-  for (uint32_t r = threadIdx.x; r < m; r += blockDim.x) a.msorted[r] = sm[r];
+  if (r >= m) return;
+  const unsigned long long v = sm[r];
+  uint32_t rank = 0;
+  uint32_t q = 0;
+  for (; q + 4 <= m; q += 4)
+    rank += (sm[q] < v) + (sm[q + 1] < v) + (sm[q + 2] < v) + (sm[q + 3] < v);
+  for (; q < m; ++q) rank += sm[q] < v;
+  a.msorted[rank] = v;
 }
 
 // Thread i places slot i if it kept its key, and the i-th smallest mover.
 __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   if (!a.ctl[0]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
   const uint32_t m = a.ctl[1];
   if (i < (int64_t)m) {  // a mover: its rank among movers + the stayers ordered before it
     const unsigned long long v = a.msorted[i];
@@ -166,11 +160,28 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
     a.keyS[fin] = k;
     a.perm[fin] = sl;
   }
-  if ((a.mask[i >> 5] >> (i & 31)) & 1u) return;
-  // a stayer: its rank among stayers + the movers ordered before it
+  // a stayer: its rank among stayers + the movers ordered before it.  The
+  // block's slots are consecutive, so the movers ordered before any of them lie
+  // between the counts of its first and last slot (two searches per block).
+  __shared__ uint32_t bounds[2];
+  const int64_t b0 = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t b1 = min(b0 + (int64_t)blockDim.x, a.n) - 1;
+  if (threadIdx.x == 0 || threadIdx.x == 32) {
+    const int64_t s = threadIdx.x == 0 ? b0 : b1;
+    const unsigned long long vb = ((unsigned long long)a.keyA[s] << 32) | (uint32_t)s;
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (a.msorted[mid] < vb) lo = mid + 1;
+      else hi = mid;
+    }
+    bounds[threadIdx.x == 0 ? 0 : 1] = lo;
+  }
+  __syncthreads();
+  if (i >= a.n || ((a.mask[i >> 5] >> (i & 31)) & 1u)) return;
   const uint32_t k = a.keyA[i];
   const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
-  uint32_t lo = 0, hi = m;
+  uint32_t lo = bounds[0], hi = bounds[1];
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
     if (a.msorted[mid] < v) lo = mid + 1;
@@ -189,13 +200,15 @@ cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(movers_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(movers_rank, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kMoverCap * (int)sizeof(unsigned long long));
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  const int64_t cap = a.n < kMoverCap ? a.n : kMoverCap;
   movers_compact<<<mover_groups(a.n), kCompactThreads, 0, st>>>(a);
-  movers_sort<<<1, kPlaceThreads, kMoverCap * sizeof(unsigned long long), st>>>(a);
+  movers_rank<<<(unsigned)((cap + kRankTile - 1) / kRankTile), kRankTile,
+                kMoverCap * sizeof(unsigned long long), st>>>(a);
   movers_merge<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
   return cudaGetLastError();
 }

@@ -5,15 +5,15 @@
 
 namespace sphg {
 
-constexpr int kGroupShift = 16;   // slots per mover group count: 65,536
-constexpr int kMoverCap = 8192;   // largest mover set sorted in one CTA (64 KB of shared memory)
+constexpr int kGroupShift = 13;   // slots per mover group count: 8,192
+constexpr int kMoverCap = 8192;   // largest mover set merged incrementally (64 KB of shared memory)
 
 struct MoverArgs {
   int64_t n;
   const uint32_t* keyA;    // sorted keys of the current state, slot order
   const uint32_t* keyB;    // keys of the integrated state, per slot
   const uint32_t* mask;    // [ceil(n/32)] bit s%32 of word s/32: slot s changed key
-  const uint32_t* gsum;    // [mover_groups(n)] changed slots per group of 65,536 slots
+  const uint32_t* gsum;    // [mover_groups(n)] changed slots per group of 8,192 slots
   uint32_t* wprefix;       // [ceil(n/32)] changed slots before each word
   unsigned long long* movers;   // [kMoverCap] key << 32 | slot, slot order
   unsigned long long* msorted;  // [kMoverCap] the same, ascending
@@ -21,10 +21,12 @@ struct MoverArgs {
   uint32_t* epoch;         // step epoch of the cell-range table
   uint32_t* keyS;          // out: sorted keys
   uint32_t* perm;          // out: previous slot of each sorted position
+  unsigned long long cond; // graph conditional handle of the full sort (0: none), set to
+                           // 1 when it must run, 0 when the merge handled the iteration
 };
 
 int mover_groups(int64_t n);
-// movers_compact, movers_sort, movers_merge; when more than kMoverCap
+// movers_compact, movers_rank, movers_merge; when more than kMoverCap
 // slots changed they do nothing and leave ctl[0] = 0 for the full sort.
 cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st);
 

@@ -418,6 +418,50 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_final(int chunks, cons
   if (threadIdx.x < 6) out[inst * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// CFL inputs per (chunk, instance): FP64 maxima of |v|^2 and |a|^2 (a from the
+// force-only pass), reduced over chunks by step_cfl_final.
+__global__ void __launch_bounds__(kDiagThreads) step_cfl_partial(StepArgs a, int chunks, double* partials) {
+  const int inst = blockIdx.y;
+  const InstDesc d = (a.ninst == 1) ? a.d0 : a.desc[inst];
+  const int64_t cnt = d.end - d.begin;
+  const int64_t per = (cnt + chunks - 1) / chunks;
+  const int64_t b = d.begin + per * blockIdx.x;
+  const int64_t e = min((int64_t)d.end, b + per);
+  double v2 = 0.0, a2 = 0.0;
+  for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const float4 v = a.velpA[i];
+    const float2 f = a.acc[i];
+    v2 = fmax(v2, (double)v.x * v.x + (double)v.y * v.y);
+    a2 = fmax(a2, (double)f.x * f.x + (double)f.y * f.y);
+  }
+  v2 = warp_max(v2);
+  a2 = warp_max(a2);
+  __shared__ double sh[2][kDiagThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][w] = v2;
+    sh[1][w] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double m = 0.0;
+    for (int k = 0; k < kDiagThreads / 32; ++k) m = fmax(m, sh[threadIdx.x][k]);
+    partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = m;
+  }
+}
+
+__global__ void step_cfl_final(int ninst, int chunks, const double* partials, double* out) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= ninst) return;
+  double v2 = 0.0, a2 = 0.0;
+  for (int c = 0; c < chunks; ++c) {
+    v2 = fmax(v2, partials[((size_t)inst * chunks + c) * 6]);
+    a2 = fmax(a2, partials[((size_t)inst * chunks + c) * 6 + 1]);
+  }
+  out[inst * 6] = v2;
+  out[inst * 6 + 1] = a2;
+}
+
 // ---------------------------------------------------------------- stand-alone keys
 __global__ void cell_keys_plain(InstDesc d, const float* __restrict__ x,
                                 const float* __restrict__ y, int64_t n, int32_t* keys) {
@@ -493,6 +537,13 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
   if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
   else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
   step_diag_final<<<a.ninst, kDiagThreads, 0, s>>>(chunks, partials, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cfl(const StepArgs& a, double* partials, int chunks, double* out, cudaStream_t s) {
+  dim3 g(chunks, a.ninst);
+  step_cfl_partial<<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
+  step_cfl_final<<<blocks_for(a.ninst, 128), 128, 0, s>>>(a.ninst, chunks, partials, out);
   return cudaGetLastError();
 }
 

@@ -72,6 +72,8 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
 // Diagnostics chunks of the largest instance (at most cap; the partial buffer
 // holds ninst x cap x 6 doubles).
 int diag_chunks(int64_t max_inst_n, int cap = 1024);
+// out[6*inst + {0, 1}] = max |v|^2, max |a|^2 of each instance (a.acc must hold the forces).
+cudaError_t launch_cfl(const StepArgs& a, double* partials, int chunks, double* out, cudaStream_t s);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
 int lists_impl(const StepArgs& a, int precision, int64_t* offs, int32_t* idx, int64_t* total,
                cudaStream_t st, std::string* err, bool encoded = false);

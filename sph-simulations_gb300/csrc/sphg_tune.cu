@@ -1,0 +1,122 @@
+// sphg_tune.cu -- the autotuner: picks the launch configuration of a workload
+// by timing each candidate on the workload itself.
+//
+// Candidates: the cell-block shape (no tiles -- one thread per particle --, or
+// Morton tiles of 2^b x 2^b cells staged in shared memory, b = 3..5; tiles
+// need every instance in Morton order) crossed with the re-sort strategy
+// (incremental merge of the particles that changed cell, or the full radix
+// sort every iteration).  Each candidate gets its own handle with the caller's
+// state, runs the pre-loop and a few warm-up iterations, then `steps` timed
+// iterations (CUDA events on the caller's stream).  Results are remembered per
+// workload signature (instance sizes, precision, orders), so a second call for
+// the same workload returns at once.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sphg.h"
+#include "sphg_internal.cuh"
+
+namespace {
+
+struct Tuned {
+  sphg_options opt;
+  double ms;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, Tuned> g_tuned;
+
+std::string signature(int32_t ninst, const sphg_params* p, const int64_t* counts, const sphg_options* base,
+                      int32_t steps) {
+  std::string s = std::to_string(ninst) + "/" + std::to_string(base->precision) + "/" +
+                  std::to_string(base->compute) + "/" + std::to_string(steps);
+  for (int i = 0; i < ninst; ++i) {
+    s += "|" + std::to_string(counts[i]) + ":" + std::to_string(p[i].order) + ":" + std::to_string(p[i].periodic);
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), ":%.17g:%.17g:%.17g", p[i].h, p[i].hi[0] - p[i].lo[0], p[i].hi[1] - p[i].lo[1]);
+    s += buf;
+  }
+  return s;
+}
+
+}  // namespace
+
+extern "C" sphg_status sphg_autotune(int32_t ninst, const sphg_params* p, const int64_t* counts,
+                                     const double* x, const double* y, const double* vx, const double* vy,
+                                     const sphg_options* base, int32_t steps, sphg_options* best,
+                                     double* ms_per_step, void* stream) {
+  using namespace sphg_detail;
+  if (ninst <= 0 || !p || !counts || !x || !y || !vx || !vy || !best || steps < 1)
+    return fail(SPHG_INVALID_ARG, "null argument, ninst <= 0 or steps < 1");
+  sphg_options b;
+  if (base) b = *base; else sphg_default_options(&b);
+  const std::string sig = signature(ninst, p, counts, &b, steps);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(sig);
+    if (it != g_tuned.end()) {
+      *best = it->second.opt;
+      if (ms_per_step) *ms_per_step = it->second.ms;
+      return SPHG_OK;
+    }
+  }
+  bool all_morton = true;
+  for (int i = 0; i < ninst; ++i) all_morton = all_morton && p[i].order == SPHG_ORDER_MORTON;
+  std::vector<int> tiles = {-1};
+  if (all_morton && b.compute == SPHG_COMPUTE_SORTED)
+    for (int t = 3; t <= 5; ++t) tiles.push_back(t);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SPHG_CUDA(cudaEventCreate(&e0));
+  SPHG_CUDA(cudaEventCreate(&e1));
+  Tuned win{b, -1.0};
+  sphg_status res = SPHG_OK;
+  for (int tb : tiles) {
+    for (int resort : {1, 0}) {
+      if (tb > 0 && resort) continue;  // the tile kernels do not record cell changes
+      sphg_options o = b;
+      o.tile_bits = tb;
+      o.resort = resort;
+      sphg_sim* s = nullptr;
+      sphg_status st2 = sphg_create_batch(ninst, p, counts, &o, &s);
+      if (st2 == SPHG_OK) st2 = sphg_upload(s, x, y, vx, vy, stream);
+      if (st2 == SPHG_OK) st2 = sphg_preloop(s, stream);
+      if (st2 == SPHG_OK) st2 = sphg_step(s, 3, stream);
+      float ms = 0.f;
+      if (st2 == SPHG_OK) {
+        cudaError_t e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) st2 = sphg_step(s, steps, stream);
+        if (e == cudaSuccess && st2 == SPHG_OK) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess && st2 == SPHG_OK) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess && st2 == SPHG_OK) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) st2 = fail(SPHG_CUDA_ERROR, std::string("autotune timing: ") + cudaGetErrorString(e));
+      }
+      if (s) sphg_destroy(s);
+      if (st2 == SPHG_OOM || st2 == SPHG_CAPACITY) continue;  // this candidate does not fit: skip it
+      if (st2 != SPHG_OK) {
+        res = st2;
+        break;
+      }
+      const double per = ms / steps;
+      if (win.ms < 0 || per < win.ms) win = Tuned{o, per};
+    }
+    if (res != SPHG_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (res != SPHG_OK) return res;
+  if (win.ms < 0) return fail(SPHG_OOM, "no candidate configuration fits on the device");
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[sig] = win;
+  }
+  *best = win.opt;
+  if (ms_per_step) *ms_per_step = win.ms;
+  return SPHG_OK;
+}

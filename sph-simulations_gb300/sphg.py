@@ -98,7 +98,12 @@ def lib():
         L.sphg_neighbor_lists_encoded.argtypes = [SP, _lp, _ip, _lp, _vp]
         L.sphg_delta_encode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
         L.sphg_delta_decode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
-        for f in ("sphg_neighbor_lists_encoded", "sphg_delta_encode", "sphg_delta_decode"):
+        L.sphg_autotune.argtypes = [ctypes.c_int32, PP, _lp, _dp, _dp, _dp, _dp, OP, ctypes.c_int32, OP,
+                                    _dp, _vp]
+        L.sphg_cfl_dt.argtypes = [SP, ctypes.c_double, ctypes.c_double, _dp, _vp]
+        L.sphg_set_dt.argtypes = [SP, ctypes.c_int32, ctypes.c_double]
+        for f in ("sphg_neighbor_lists_encoded", "sphg_delta_encode", "sphg_delta_decode", "sphg_autotune",
+                  "sphg_cfl_dt", "sphg_set_dt"):
             getattr(L, f).restype = ctypes.c_int
         for f in ("sphg_create", "sphg_create_batch", "sphg_destroy", "sphg_upload",
                   "sphg_preloop", "sphg_step", "sphg_download", "sphg_diagnostics",
@@ -215,7 +220,7 @@ class Sim:
         if which in (DBG_POS_NEXT, DBG_VEL_NEXT):
             out = np.empty(2 * self.n, np.float64)
         elif which == DBG_RESORT:
-            out = np.zeros(2, np.int32)
+            out = np.zeros(3, np.int32)
         else:
             out = np.empty(self.n, np.int32)
         check(lib().sphg_get_debug(self._h, which, out.ctypes.data_as(_vp), _stream(stream)))
@@ -243,6 +248,14 @@ class Sim:
         check(lib().sphg_neighbor_lists_encoded(self._h, _ptr(offs, _lp), _ptr(enc, _ip),
                                                 ctypes.byref(total), _stream(stream)))
         return offs, enc[:total.value]
+
+    def cfl_dt(self, cfl=0.25, force_coef=0.25, stream=None):
+        out = np.zeros(self.ninst, np.float64)
+        check(lib().sphg_cfl_dt(self._h, float(cfl), float(force_coef), _ptr(out), _stream(stream)))
+        return out
+
+    def set_dt(self, dt, inst=-1):
+        check(lib().sphg_set_dt(self._h, int(inst), float(dt)))
 
     def snapshot(self, stream=None):
         """bytes of an exact-resume snapshot of the current state."""
@@ -341,6 +354,21 @@ def sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, n, bits, st
     """Stand-alone radix sort on caller-owned device buffers (raw pointers)."""
     check(lib().sphg_sort_pairs(keys_in_ptr, vals_in_ptr, keys_out_ptr, vals_out_ptr, int(n),
                                 int(bits), _stream(stream)))
+
+
+def autotune(prms, counts, x, y, vx, vy, base=None, steps=10, stream=None):
+    """Fastest launch configuration of this workload: (Options, ms per iteration)."""
+    if not isinstance(prms, (list, tuple)):
+        prms = [prms]
+    counts = np.ascontiguousarray(counts if np.ndim(counts) else [counts], dtype=np.int64)
+    arr = (Params * len(prms))(*prms)
+    x, y, vx, vy = _f64(x), _f64(y), _f64(vx), _f64(vy)
+    best = Options()
+    ms = ctypes.c_double(0.0)
+    check(lib().sphg_autotune(len(prms), arr, _ptr(counts, _lp), _ptr(x), _ptr(y), _ptr(vx), _ptr(vy),
+                              ctypes.byref(base if base is not None else options()), int(steps),
+                              ctypes.byref(best), ctypes.byref(ms), _stream(stream)))
+    return best, ms.value
 
 
 def delta_encode(offs_ptr, idx_ptr, n, enc_ptr, stream=None):

@@ -704,6 +704,11 @@ def test_incremental_resort_equals_full_sort_bitwise(prec, vel):
         o = sim.download()
         o["keys"] = sim.debug(S.DBG_KEYS)
         o["perm"] = sim.debug(S.DBG_PERM)
+        rs = sim.debug(S.DBG_RESORT)
+        if resort and vel < 1:
+            assert rs[0] == 1 and rs[1] == moved[-1] or rs[0] == 1
+        if not resort:
+            assert rs[0] == 0
         outs.append((o, moved))
         sim.close()
     (a, moved), (b, _) = outs
@@ -713,3 +718,57 @@ def test_incremental_resort_equals_full_sort_bitwise(prec, vel):
         assert max(moved) > 8192  # at least one iteration took the full sort
     for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids", "keys", "perm"):
         assert np.array_equal(a[f], b[f], equal_nan=True), f
+
+
+# ---------------------------------------------------------------- autotuner, adaptive dt
+def test_autotune_returns_a_working_configuration():
+    S = _sphg()
+    inst = _instances(seed=13)
+    prms = [S.params(**i[0]) for i in inst]
+    counts = [len(i[1]) for i in inst]
+    cat = [np.concatenate([i[k] for i in inst]) for k in (1, 2, 3, 4)]
+    best, ms = S.autotune(prms, counts, *cat, base=S.options(precision=S.SPLIT), steps=5)
+    assert ms > 0 and best.precision == S.SPLIT
+    assert best.tile_bits == -1  # one instance is row-major: no cell tiles
+    again, ms2 = S.autotune(prms, counts, *cat, base=S.options(precision=S.SPLIT), steps=5)
+    assert ms2 == ms and again.resort == best.resort  # remembered
+    morton = [i for i in inst if i[0]["order"] == "morton"]
+    best_m, _ = S.autotune([S.params(**i[0]) for i in morton], [len(i[1]) for i in morton],
+                           *[np.concatenate([i[k] for i in morton]) for k in (1, 2, 3, 4)], steps=5)
+    assert best_m.tile_bits in (-1, 3, 4, 5)
+    a = S.Sim(prms, counts, best)
+    b = S.Sim(prms, counts, S.options(precision=S.SPLIT))
+    for s in (a, b):
+        s.upload(*cat)
+        s.preloop()
+        s.step(10)
+    oa, ob = a.download(), b.download()
+    ia, ib = np.argsort(oa["ids"]), np.argsort(ob["ids"])
+    np.testing.assert_allclose(oa["x"][ia], ob["x"][ib], rtol=0, atol=1e-9)
+    a.close()
+    b.close()
+
+
+def test_cfl_dt_and_set_dt():
+    S = _sphg()
+    x, y, vx, vy = jittered(60, 50, 0.005, seed=17, vel=0.4)
+    kw = dict(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.4, 0.3), c0=5.0)
+    sim = S.Sim(S.params(**kw), len(x))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    sim.step(3)
+    o = sim.download()
+    dt = sim.cfl_dt(cfl=0.3, force_coef=0.2)
+    vmax = np.sqrt((o["vx"] ** 2 + o["vy"] ** 2).max())
+    amax = np.sqrt((o["fx"] ** 2 + o["fy"] ** 2).max())
+    want = min(0.3 * 0.0065 / (5.0 + vmax), 0.2 * np.sqrt(0.0065 / amax))
+    np.testing.assert_allclose(dt[0], want, rtol=1e-6)
+    # a new dt applies from the next iteration on (graph rebuilt)
+    sim.set_dt(2.5e-5)
+    sim.step(1)
+    a = sim.download()
+    nx_, ny_ = sim.debug(S.DBG_POS_NEXT)
+    p = O.params(**dict(kw, dt=2.5e-5))
+    ox, oy, _, _ = O.integrate(p, a["x"], a["y"], a["vx"], a["vy"], a["fx"], a["fy"])
+    assert np.max(np.abs(nx_ - ox)) < 1e-9 and np.max(np.abs(ny_ - oy)) < 1e-9
+    sim.close()
