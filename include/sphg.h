@@ -127,6 +127,26 @@ sphg_status sphg_destroy(sphg_sim* s);
 /* Host arrays of all instances' particles concatenated (instance order). */
 sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const double* vx,
                         const double* vy, void* stream);
+/* Initial state generated on the device, one lattice per instance: the
+ * reference's LatticeCreator (core/container/Lattice.h:12-35: x = x0 + i dx,
+ * y = y0 + j dy, particle i + nx j) with an optional seeded uniform jitter of
+ * +-jitter spacings and an optional Taylor-Green velocity field
+ * (vx = u0 sin(2 pi x/Lx) cos(2 pi y/Ly), vy = -u0 cos(2 pi x/Lx) sin(2 pi y/Ly),
+ * x and y measured from lo).  nx * ny must equal the instance's particle
+ * count.  Replaces sphg_upload; no host arrays are involved. */
+enum { SPHG_VEL_ZERO = 0, SPHG_VEL_TAYLOR_GREEN = 1 };
+typedef struct sphg_lattice {
+  double x0, y0;    /* first point */
+  double dx, dy;    /* spacing */
+  int64_t nx, ny;   /* points per direction */
+  double jitter;    /* uniform jitter amplitude in spacings (0 = none) */
+  uint64_t seed;    /* jitter stream */
+  int32_t velocity; /* SPHG_VEL_* */
+  int32_t pad;
+  double u0;        /* Taylor-Green amplitude */
+} sphg_lattice;
+sphg_status sphg_upload_lattice(sphg_sim* s, const sphg_lattice* spec, void* stream);
+
 /* FindNeighbors -> density -> pressure -> forces of the initial state. */
 sphg_status sphg_preloop(sphg_sim* s, void* stream);
 /* nsteps main-loop iterations: integrate -> FindNeighbors -> density -> pressure -> forces. */

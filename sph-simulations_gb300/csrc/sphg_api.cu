@@ -735,6 +735,19 @@ sphg_status sphg_step(sphg_sim* s, int64_t nsteps, void* stream) {
   return run_steps(s, nsteps, (cudaStream_t)stream);
 }
 
+// Error words the kernels set instead of faulting or hanging: the radix sort's
+// look-back (a wait that gave up) and the incremental re-sort's consistency
+// word.  Read at the synchronising calls; both stay set.
+static sphg_status device_errors(sphg_sim* s, cudaStream_t st) {
+  uint32_t w[2] = {0, 0};
+  SPHG_CUDA(cudaMemcpyAsync(&w[0], sphg::sort_error_word(s->scratch), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(&w[1], s->flags + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaStreamSynchronize(st));
+  if (w[0]) return fail(SPHG_TIMEOUT, "a radix-sort look-back wait gave up; the state is not valid");
+  if (w[1]) return fail(SPHG_CUDA_ERROR, "inconsistent incremental re-sort record; the state is not valid");
+  return SPHG_OK;
+}
+
 sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double* vy, double* rho,
                           double* fx, double* fy, int32_t* ids, void* stream) {
   if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state to download");
@@ -762,6 +775,7 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
   if (ids && s->opt.track_ids)
     SPHG_CUDA(cudaMemcpyAsync(ids, s->idsA, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
+  SPHG_TRY(device_errors(s, st));
   if (ids && !s->opt.track_ids)
     for (int64_t i = 0; i < n; ++i) ids[i] = -1;
   parallel_for(n, [&](int64_t b, int64_t e) {
@@ -804,7 +818,7 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream) {
   SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst,
                             cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
-  return SPHG_OK;
+  return device_errors(s, st);
 }
 
 sphg_status sphg_cfl_dt(sphg_sim* s, double cfl, double force_coef, double* out, void* stream) {

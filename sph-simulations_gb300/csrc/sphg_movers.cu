@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
       const int b = __ffs(bits) - 1;
       bits &= bits - 1;
       const uint32_t slot = (uint32_t)((w << 5) + b);
-      a.movers[r] = ((uint64_t)a.keyB[slot] << 32) | slot;
+      if (r < tot && slot < a.n) a.movers[r] = ((uint64_t)a.keyB[slot] << 32) | slot;
+      else a.ctl[2] = 1u;  // inconsistent mover record: nothing is written out of bounds
       ++r;
     }
   }
@@ -144,7 +145,8 @@ __global__ void __launch_bounds__(kRankTile) movers_rank(MoverArgs a) {
   for (; q + 4 <= m; q += 4)
     rank += (sm[q] < v) + (sm[q + 1] < v) + (sm[q + 2] < v) + (sm[q + 3] < v);
   for (; q < m; ++q) rank += sm[q] < v;
-  a.msorted[rank] = v;
+  if (rank < m) a.msorted[rank] = v;
+  else a.ctl[2] = 1u;
 }
 
 // Thread i places slot i if it kept its key, and the i-th smallest mover.
@@ -157,8 +159,12 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
     const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
     const int64_t p = slots_before(a, k, sl);
     const int64_t fin = i + (p - (int64_t)movers_before(a, p, m));
-    a.keyS[fin] = k;
-    a.perm[fin] = sl;
+    if (fin >= 0 && fin < a.n) {
+      a.keyS[fin] = k;
+      a.perm[fin] = sl;
+    } else {
+      a.ctl[2] = 1u;
+    }
   }
   // a stayer: its rank among stayers + the movers ordered before it.  The
   // block's slots are consecutive, so the movers ordered before any of them lie
@@ -188,8 +194,12 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
     else hi = mid;
   }
   const int64_t fin = i - (int64_t)movers_before(a, i, m) + lo;
-  a.keyS[fin] = k;
-  a.perm[fin] = (uint32_t)i;
+  if (fin >= 0 && fin < a.n) {
+    a.keyS[fin] = k;
+    a.perm[fin] = (uint32_t)i;
+  } else {
+    a.ctl[2] = 1u;
+  }
 }
 
 }  // namespace

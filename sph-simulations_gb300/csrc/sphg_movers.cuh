@@ -17,7 +17,8 @@ struct MoverArgs {
   uint32_t* wprefix;       // [ceil(n/32)] changed slots before each word
   unsigned long long* movers;   // [kMoverCap] key << 32 | slot, slot order
   unsigned long long* msorted;  // [kMoverCap] the same, ascending
-  uint32_t* ctl;           // [0] = 1 when the incremental path ran, [1] = changed slots
+  uint32_t* ctl;           // [0] = 1 when the incremental path ran, [1] = changed slots,
+                           // [2] set to 1 if a record was inconsistent (never cleared here)
   uint32_t* epoch;         // step epoch of the cell-range table
   uint32_t* keyS;          // out: sorted keys
   uint32_t* perm;          // out: previous slot of each sorted position

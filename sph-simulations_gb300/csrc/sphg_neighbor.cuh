@@ -164,6 +164,11 @@ __device__ __forceinline__ void stencil_keys(const InstDesc& d, uint32_t code, i
 // the main pass and decided by a second pass over the same cells, which keeps
 // the FP64 code out of the hot loop; only the summation order of those rare
 // pairs differs.
+#ifndef SPHG_CELL_BATCH
+#define SPHG_CELL_BATCH 2
+#endif
+constexpr int kCellBatch = SPHG_CELL_BATCH;  // particles of a cell whose loads are issued together
+
 template <int PREC, bool ORDERED = false, class F>
 __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstDesc& d,
                                                   uint32_t key, float2 pi, int& cx, int& cy,
@@ -194,13 +199,12 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
     const bool wrapped = (PREC == 0) && ((wrapmask >> k) & 1u);
     const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
     const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
-    for (uint32_t j = rs[k]; j < re[k]; ++j) {
-      const float2 pj = __ldg(pos + j);
+    auto candidate = [&](uint32_t j, float2 pj) {
       float dx = (pi.x - pj.x) - shx;
       float dy = (pi.y - pj.y) - shy;
       if (wrapped) {
         if (wrapped_pair(d, pi, pj, dx, dy)) visit(j, dx, dy, fmaf(dx, dx, dy * dy), (uint32_t)k | 16u);
-        continue;
+        return;
       }
       const float r2 = fmaf(dx, dx, dy * dy);
       if (r2 < d.h2_lo) {
@@ -212,7 +216,17 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
           border = true;
         }
       }
-    }
+    };
+    // the first kCellBatch particles of the cell: their loads are issued together
+    const uint32_t s0 = rs[k], e0 = re[k];
+    float2 pb[kCellBatch];
+#pragma unroll
+    for (int u = 0; u < kCellBatch; ++u)
+      pb[u] = (s0 + u < e0) ? __ldg(pos + s0 + u) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kCellBatch; ++u)
+      if (s0 + u < e0) candidate(s0 + u, pb[u]);
+    for (uint32_t j = s0 + kCellBatch; j < e0; ++j) candidate(j, __ldg(pos + j));
   }
   if (ORDERED || !border) return;
 #pragma unroll 1

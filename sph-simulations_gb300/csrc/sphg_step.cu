@@ -21,6 +21,7 @@
 #include <type_traits>
 #include <cuda_runtime.h>
 
+#include "sphg_movers.cuh"
 #include "sphg_neighbor.cuh"
 #include "sphg_step.cuh"
 
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 // list: the warp executes the heavy per-pair math about max-over-lanes(count)
 // times instead of once per candidate iteration.  A thread with more than
 // kForceBuf neighbours handles the extra ones inline during the scan.
+static_assert(((1 << kGroupShift) % kThreads) == 0, "a force block lies inside one mover group");
 constexpr int kForceBuf = 12;
 #ifndef SPHG_FORCE_BATCH
 #define SPHG_FORCE_BATCH 4
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
     }
     __syncthreads();
     if (threadIdx.x == 0 && moved_in_block)
-      atomicAdd(a.mover_gsum + (((int64_t)blockIdx.x * blockDim.x) >> 16), moved_in_block);
+      atomicAdd(a.mover_gsum + (((int64_t)blockIdx.x * blockDim.x) >> kGroupShift), moved_in_block);
   }
 }
 

@@ -38,6 +38,21 @@ class Params(ctypes.Structure):
     ]
 
 
+class Lattice(ctypes.Structure):
+    _fields_ = [("x0", ctypes.c_double), ("y0", ctypes.c_double), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("nx", ctypes.c_int64), ("ny", ctypes.c_int64),
+                ("jitter", ctypes.c_double), ("seed", ctypes.c_uint64), ("velocity", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("u0", ctypes.c_double)]
+
+
+VEL_ZERO, VEL_TAYLOR_GREEN = 0, 1
+
+
+def lattice(x0, y0, dx, dy, nx, ny, jitter=0.0, seed=0, velocity=VEL_ZERO, u0=0.0):
+    return Lattice(float(x0), float(y0), float(dx), float(dy), int(nx), int(ny), float(jitter),
+                   int(seed) & 0xFFFFFFFFFFFFFFFF, int(velocity), 0, float(u0))
+
+
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
@@ -100,6 +115,8 @@ def lib():
         L.sphg_delta_decode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
         L.sphg_autotune.argtypes = [ctypes.c_int32, PP, _lp, _dp, _dp, _dp, _dp, OP, ctypes.c_int32, OP,
                                     _dp, _vp]
+        L.sphg_upload_lattice.argtypes = [SP, ctypes.POINTER(Lattice), _vp]
+        L.sphg_upload_lattice.restype = ctypes.c_int
         L.sphg_cfl_dt.argtypes = [SP, ctypes.c_double, ctypes.c_double, _dp, _vp]
         L.sphg_set_dt.argtypes = [SP, ctypes.c_int32, ctypes.c_double]
         for f in ("sphg_neighbor_lists_encoded", "sphg_delta_encode", "sphg_delta_decode", "sphg_autotune",
@@ -189,6 +206,13 @@ class Sim:
         x, y, vx, vy = _f64(x), _f64(y), _f64(vx), _f64(vy)
         assert len(x) == self.n
         check(lib().sphg_upload(self._h, _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _stream(stream)))
+
+    def upload_lattice(self, specs, stream=None):
+        """Device-generated initial state: one Lattice per instance."""
+        if isinstance(specs, Lattice):
+            specs = [specs]
+        arr = (Lattice * len(specs))(*specs)
+        check(lib().sphg_upload_lattice(self._h, arr, _stream(stream)))
 
     def preloop(self, stream=None):
         check(lib().sphg_preloop(self._h, _stream(stream)))
