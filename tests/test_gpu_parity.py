@@ -753,7 +753,7 @@ def test_cfl_dt_and_set_dt():
     S = _sphg()
     x, y, vx, vy = jittered(60, 50, 0.005, seed=17, vel=0.4)
     kw = dict(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.4, 0.3), c0=5.0)
-    sim = S.Sim(S.params(**kw), len(x))
+    sim = S.Sim(S.params(**kw), len(x), S.options(precision=S.SPLIT))  # positions to ~1e-10
     sim.upload(x, y, vx, vy)
     sim.preloop()
     sim.step(3)
