@@ -305,7 +305,8 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
   if (ev) SPHG_CUDA(cudaEventRecord(ev[1], st));
   // the force pass of the previous iteration recorded which slots changed
   // cell: merge them in when few did (the full sort's kernels then skip)
-  const bool inc = s->movers_on && !first;
+  const bool inc = s->movers_on && !first && !s->force_full_sort;
+  s->force_full_sort = false;
   if (inc) SPHG_TRY(enqueue_movers(s, st, 0));
   SPHG_TRY(enqueue_full_sort(s, st, inc ? s->flags + 3 : nullptr));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));

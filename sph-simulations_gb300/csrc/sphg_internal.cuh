@@ -66,6 +66,7 @@ struct sphg_sim {
   int64_t csr_cap = 0, csr_total = 0;
   // incremental re-sort: mover bits and group counts written by the force pass
   bool movers_on = false;
+  bool force_full_sort = false;  // the next iteration sorts fully (the slot record is stale)
   uint32_t *mmask = nullptr, *mgsum = nullptr, *mwprefix = nullptr;
   unsigned long long *mlist = nullptr, *msorted = nullptr;
   int mgroups = 0;

@@ -16,8 +16,9 @@
 // same decision word and skip themselves otherwise).
 //
 // Kernels: movers_compact (mover list in slot order, movers before each word,
-// decision), movers_rank (each mover's rank by counting the smaller ones),
-// movers_merge (final position of every stayer and every mover).
+// decision), movers_rank_place (a warp per mover: its rank by counting the
+// smaller movers, its final position by a warp-wide search of the slots),
+// movers_merge (final position of every stayer).
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -31,7 +32,7 @@ namespace {
 constexpr int kCompactThreads = 256;
 constexpr int kCompactWords = 1;  // words per thread: 256 x 1 word = one group of 8,192 slots
 static_assert(kCompactThreads * kCompactWords * 32 == (1 << kGroupShift), "one block per group");
-constexpr int kRankTile = 128;
+constexpr int kRankThreads = 256;  // 8 movers per block
 constexpr int kStayThreads = 256;
 
 __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p, uint32_t m) {
@@ -114,58 +115,62 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
   }
 }
 
-// Number of slots s with (keyA[s], s) < (k, sl): the slots are in that order.
-__device__ __forceinline__ int64_t slots_before(const MoverArgs& a, uint32_t k, uint32_t sl) {
-  int64_t lo = 0, hi = a.n;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    const uint32_t km = a.keyA[mid];
-    if (km < k || (km == k && mid < (int64_t)sl)) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// Rank of each mover among the movers = how many (key, slot) pairs are smaller
-// (all distinct); the mover list is staged in shared memory once per CTA and
-// every thread counts against all of it.  kRankTile movers per CTA; CTAs past
-// the mover count exit.
-__global__ void __launch_bounds__(kRankTile) movers_rank(MoverArgs a) {
-  extern __shared__ unsigned long long sm[];
+// One warp per mover: its rank among the movers (the lanes split the
+// comparisons against the whole mover list, L1-cached), then its final
+// position = rank + the stayers ordered before it, found by a warp-wide
+// 32-way search of the slots' (key, slot) order (four or five dependent
+// rounds instead of twenty for a million slots).
+__global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
   if (!a.ctl[0]) return;
   const uint32_t m = a.ctl[1];
-  const uint32_t r = blockIdx.x * kRankTile + threadIdx.x;
-  if (blockIdx.x * kRankTile >= m) return;
-  for (uint32_t q = threadIdx.x; q < m; q += blockDim.x) sm[q] = a.movers[q];
-  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const uint32_t r = blockIdx.x * (kRankThreads / 32) + (threadIdx.x >> 5);
   if (r >= m) return;
-  const unsigned long long v = sm[r];
-  uint32_t rank = 0;
-  uint32_t q = 0;
-  for (; q + 4 <= m; q += 4)
-    rank += (sm[q] < v) + (sm[q + 1] < v) + (sm[q + 2] < v) + (sm[q + 3] < v);
-  for (; q < m; ++q) rank += sm[q] < v;
-  if (rank < m) a.msorted[rank] = v;
-  else a.ctl[2] = 1u;
-}
-
-// Thread i places slot i if it kept its key, and the i-th smallest mover.
-__global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
-  if (!a.ctl[0]) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t m = a.ctl[1];
-  if (i < (int64_t)m) {  // a mover: its rank among movers + the stayers ordered before it
-    const unsigned long long v = a.msorted[i];
-    const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
-    const int64_t p = slots_before(a, k, sl);
-    const int64_t fin = i + (p - (int64_t)movers_before(a, p, m));
-    if (fin >= 0 && fin < a.n) {
+  const unsigned long long v = __ldg(a.movers + r);
+  uint32_t c = 0;
+  for (uint32_t q = lane; q < m; q += 32) c += __ldg(a.movers + q) < v;
+  const uint32_t rank = __reduce_add_sync(0xffffffffu, c);
+  const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
+  // p = number of slots s with (keyA[s], s) < (k, sl)
+  int64_t lo = 0, hi = a.n;
+  while (hi - lo > 32) {
+    const int64_t step = (hi - lo + 31) / 32;
+    const int64_t pos = lo + (int64_t)(lane + 1) * step - 1;
+    bool less = false;
+    if (pos < hi) {
+      const uint32_t kp = a.keyA[pos];
+      less = kp < k || (kp == k && pos < (int64_t)sl);
+    }
+    const int cnt = __popc(__ballot_sync(0xffffffffu, less));
+    const int64_t nlo = lo + (int64_t)cnt * step;
+    const int64_t nhi = lo + (int64_t)(cnt + 1) * step - 1;
+    lo = nlo;
+    if (nhi < hi) hi = nhi;
+  }
+  bool less = false;
+  if (lo + lane < hi) {
+    const int64_t pos = lo + lane;
+    const uint32_t kp = a.keyA[pos];
+    less = kp < k || (kp == k && pos < (int64_t)sl);
+  }
+  const int64_t p = lo + __popc(__ballot_sync(0xffffffffu, less));
+  if (lane == 0) {
+    if (rank < m) a.msorted[rank] = v;
+    const int64_t fin = (int64_t)rank + (p - (int64_t)movers_before(a, p, m));
+    if (rank < m && fin >= 0 && fin < a.n) {
       a.keyS[fin] = k;
       a.perm[fin] = sl;
     } else {
       a.ctl[2] = 1u;
     }
   }
+}
+
+// Thread i places slot i if it kept its key (the movers are placed already).
+__global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
+  if (!a.ctl[0]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t m = a.ctl[1];
   // a stayer: its rank among stayers + the movers ordered before it.  The
   // block's slots are consecutive, so the movers ordered before any of them lie
   // between the counts of its first and last slot (two searches per block).
@@ -208,17 +213,10 @@ int mover_groups(int64_t n) { return (int)((n + (1 << kGroupShift) - 1) >> kGrou
 
 cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(movers_rank, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         kMoverCap * (int)sizeof(unsigned long long));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
   const int64_t cap = a.n < kMoverCap ? a.n : kMoverCap;
+  const int per_block = kRankThreads / 32;
   movers_compact<<<mover_groups(a.n), kCompactThreads, 0, st>>>(a);
-  movers_rank<<<(unsigned)((cap + kRankTile - 1) / kRankTile), kRankTile,
-                kMoverCap * sizeof(unsigned long long), st>>>(a);
+  movers_rank_place<<<(unsigned)((cap + per_block - 1) / per_block), kRankThreads, 0, st>>>(a);
   movers_merge<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
   return cudaGetLastError();
 }

@@ -6,7 +6,7 @@
 namespace sphg {
 
 constexpr int kGroupShift = 13;   // slots per mover group count: 8,192
-constexpr int kMoverCap = 8192;   // largest mover set merged incrementally (64 KB of shared memory)
+constexpr int kMoverCap = 8192;   // largest mover set merged incrementally
 
 struct MoverArgs {
   int64_t n;
@@ -27,7 +27,7 @@ struct MoverArgs {
 };
 
 int mover_groups(int64_t n);
-// movers_compact, movers_rank, movers_merge; when more than kMoverCap
+// movers_compact, movers_rank_place, movers_merge; when more than kMoverCap
 // slots changed they do nothing and leave ctl[0] = 0 for the full sort.
 cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st);
 

@@ -293,7 +293,6 @@ sphg_status sphg_server_create(double hbm_budget_bytes, int32_t max_instances, c
   sim->opt.use_graph = 0;    // ... and direct launches
   sim->force_batched = 1;    // same kernels (and bits) whatever the batch size
   sim->opt.compute = SPHG_COMPUTE_SORTED;
-  sim->opt.resort = 0;       // a repack invalidates the changed-slot record of the last force pass
   sphg_status st = check_options(sim, 0, nullptr);
   if (st != SPHG_OK) {
     delete sim;
@@ -394,6 +393,7 @@ sphg_status sphg_server_tick(sphg_server* s, void* stream, int32_t* live_out, in
     SPHG_TRY(repack(s, newlive, nadmit, st));
     s->live = newlive;
     s->dirty = false;
+    s->sim->force_full_sort = true;  // the last force pass's changed-slot record is of the old layout
   }
   int32_t finished = 0;
   if (!s->live.empty()) {
