@@ -199,6 +199,23 @@ def time_steps(sim, sphg, steps, stream, flush):
     return float(sum(a.elapsed_time(b) for a, b in ev))
 
 
+def max_over_ranks(x, device="cuda"):
+    """The largest per-rank value over all ranks (the timed region of the slowest
+    replica); the value itself when not running distributed."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(particles_per_replica, world, steps, max_ms):
+    """Whole-job particle-steps/s of `world` independent replicas (weak scaling)."""
+    return particles_per_replica * world * steps / (max_ms * 1e-3)
+
+
 def run_gpu(args):
     import torch
     import sphg
@@ -239,12 +256,9 @@ def run_gpu(args):
     time.sleep(0.3)
     total_ms = time_steps(sim, sphg, args.steps, stream, flush)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms)
     ms_per_step = total_ms / args.steps
-    value = n * world * args.steps / (total_ms * 1e-3)
+    value = replica_throughput(n, world, args.steps, total_ms)
 
     # ---- per-phase profile (CUDA events between the kernels of one iteration)
     phases, resort = [], []
