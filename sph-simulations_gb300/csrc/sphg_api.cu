@@ -258,9 +258,10 @@ sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
+  // group counts of this iteration's force pass (the re-sort has read the last ones)
+  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->mgsum, 0, sizeof(uint32_t) * s->mgroups, st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[3], st));
-  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->mgsum, 0, sizeof(uint32_t) * s->mgroups, st));
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
     // AssembleNeighborList: count, offsets, fill -- then density and forces over the lists
     SPHG_CUDA(sphg::launch_lists_count_scan(a, prec, s->csr_counts, s->csr_offs, s->csr_sums, st));

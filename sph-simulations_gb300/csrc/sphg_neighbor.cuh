@@ -164,11 +164,6 @@ __device__ __forceinline__ void stencil_keys(const InstDesc& d, uint32_t code, i
 // the main pass and decided by a second pass over the same cells, which keeps
 // the FP64 code out of the hot loop; only the summation order of those rare
 // pairs differs.
-#ifndef SPHG_CELL_BATCH
-#define SPHG_CELL_BATCH 2
-#endif
-constexpr int kCellBatch = SPHG_CELL_BATCH;  // particles of a cell whose loads are issued together
-
 template <int PREC, bool ORDERED = false, class F>
 __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstDesc& d,
                                                   uint32_t key, float2 pi, int& cx, int& cy,
@@ -217,16 +212,7 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
         }
       }
     };
-    // the first kCellBatch particles of the cell: their loads are issued together
-    const uint32_t s0 = rs[k], e0 = re[k];
-    float2 pb[kCellBatch];
-#pragma unroll
-    for (int u = 0; u < kCellBatch; ++u)
-      pb[u] = (s0 + u < e0) ? __ldg(pos + s0 + u) : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < kCellBatch; ++u)
-      if (s0 + u < e0) candidate(s0 + u, pb[u]);
-    for (uint32_t j = s0 + kCellBatch; j < e0; ++j) candidate(j, __ldg(pos + j));
+    for (uint32_t j = rs[k]; j < re[k]; ++j) candidate(j, __ldg(pos + j));
   }
   if (ORDERED || !border) return;
 #pragma unroll 1
