@@ -239,6 +239,12 @@ sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond
   m.keyS = s->keyTmp;
   m.perm = s->perm;
   m.cond = cond;
+  m.posB = s->posB;
+  m.velB = s->velB;
+  m.idsB = s->opt.track_ids ? s->idsB : nullptr;
+  m.posA = s->posA;
+  m.velpA = s->velpA;
+  m.idsA = s->opt.track_ids ? s->idsA : nullptr;
   SPHG_CUDA(sphg::launch_movers(m, st));
   return SPHG_OK;
 }
@@ -309,6 +315,8 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
   const bool inc = s->movers_on && !first && !s->force_full_sort;
   s->force_full_sort = false;
   if (inc) SPHG_TRY(enqueue_movers(s, st, 0));
+  // without the merge this iteration, its decision word must read "full sort"
+  else if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->flags + 3, 0, sizeof(uint32_t), st));
   SPHG_TRY(enqueue_full_sort(s, st, inc ? s->flags + 3 : nullptr));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));
   return enqueue_after_sort(s, st, ev);
@@ -482,6 +490,7 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
   auto layout = [&](Arena& A) {
     s->ddesc = A.take<InstDesc>(ninst);
     s->dbegins = A.take<int32_t>(ninst);
+    s->dinst_tab = A.take<int32_t>((N >> sphg::kInstTabShift) + 2);
     s->posA = A.take<float2>(N);
     s->posB = A.take<float2>(N);
     s->velB = A.take<float2>(N);
@@ -565,12 +574,22 @@ sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int
     cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
   }
+  // instance of the first slot of every 256-slot block
+  const int64_t blocks = (s->n >> sphg::kInstTabShift) + 1;
+  s->hinst_tab.assign((size_t)blocks, 0);
+  for (int64_t b = 0, k = 0; b < blocks; ++b) {
+    const int64_t slot = b << sphg::kInstTabShift;
+    while (k + 1 < ninst && s->hbegins[k + 1] <= slot) ++k;
+    s->hinst_tab[b] = (int32_t)k;
+  }
   if (stream) {
     SPHG_CUDA(cudaMemcpyAsync(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice, *stream));
     SPHG_CUDA(cudaMemcpyAsync(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice, *stream));
+    SPHG_CUDA(cudaMemcpyAsync(s->dinst_tab, s->hinst_tab.data(), sizeof(int32_t) * blocks, cudaMemcpyHostToDevice, *stream));
   } else {
     SPHG_CUDA(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice));
     SPHG_CUDA(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice));
+    SPHG_CUDA(cudaMemcpy(s->dinst_tab, s->hinst_tab.data(), sizeof(int32_t) * blocks, cudaMemcpyHostToDevice));
   }
   return SPHG_OK;
 }

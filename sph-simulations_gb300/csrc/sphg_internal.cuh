@@ -40,6 +40,7 @@ struct sphg_sim {
   std::vector<int64_t> counts;
   std::vector<InstDesc> hdesc;
   std::vector<int32_t> hbegins;
+  std::vector<int32_t> hinst_tab;
   uint64_t total_keys = 0;
   int key_bits = 1;
   int diag_chunks = 1;
@@ -47,6 +48,7 @@ struct sphg_sim {
   // device buffers
   InstDesc* ddesc = nullptr;
   int32_t* dbegins = nullptr;
+  int32_t* dinst_tab = nullptr;  // instance of the first slot of each 256-slot block
   float2 *posA = nullptr, *posB = nullptr, *velB = nullptr, *acc = nullptr;
   float4* velpA = nullptr;
   float* rho = nullptr;
@@ -93,6 +95,7 @@ struct sphg_sim {
     if (!hdesc.empty()) a.d0 = hdesc[0];
     a.desc = ddesc;
     a.begins = dbegins;
+    a.inst_tab = dinst_tab;
     a.posA = posA;
     a.velpA = velpA;
     a.rho = rho;
@@ -122,6 +125,7 @@ struct sphg_sim {
     a.csr_offs = csr_offs;
     a.csr_idx = csr_idx;
     a.keyS = keyTmp;
+    a.merged = movers_on ? flags + 3 : nullptr;
     a.mover_mask = movers_on ? mmask : nullptr;
     a.mover_gsum = movers_on ? mgsum : nullptr;
     return a;

@@ -42,6 +42,33 @@ __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p,
   return a.wprefix[w] + __popc(a.mask[w] & below);
 }
 
+// Slot `from` of the integrated state to sorted position `to`.
+__device__ __forceinline__ void place(const MoverArgs& a, int64_t from, int64_t to, uint32_t key) {
+  a.keyS[to] = key;
+  a.perm[to] = (uint32_t)from;
+  a.posA[to] = a.posB[from];
+  const float2 v = a.velB[from];
+  a.velpA[to] = make_float4(v.x, v.y, 0.f, 0.f);
+  if (a.idsA) a.idsA[to] = a.idsB[from];
+}
+
+// Movers ordered before v (a count in [lo, hi] of the sorted mover list), by a
+// warp-wide 32-way search: two or three dependent rounds for 8,192 movers.
+__device__ __forceinline__ uint32_t warp_count_below(const unsigned long long* __restrict__ ms, uint32_t lo,
+                                                     uint32_t hi, unsigned long long v, int lane) {
+  while (hi - lo > 32) {
+    const uint32_t step = (hi - lo + 31) / 32;
+    const uint32_t pos = lo + (uint32_t)(lane + 1) * step - 1;
+    const bool less = pos < hi && __ldg(ms + pos) < v;
+    const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, less));
+    const uint32_t nhi = lo + (cnt + 1) * step - 1;
+    lo += cnt * step;
+    if (nhi < hi) hi = nhi;
+  }
+  const bool less = lo + (uint32_t)lane < hi && __ldg(ms + lo + lane) < v;
+  return lo + __popc(__ballot_sync(0xffffffffu, less));
+}
+
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -157,12 +184,8 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
   if (lane == 0) {
     if (rank < m) a.msorted[rank] = v;
     const int64_t fin = (int64_t)rank + (p - (int64_t)movers_before(a, p, m));
-    if (rank < m && fin >= 0 && fin < a.n) {
-      a.keyS[fin] = k;
-      a.perm[fin] = sl;
-    } else {
-      a.ctl[2] = 1u;
-    }
+    if (rank < m && fin >= 0 && fin < a.n && sl < a.n) place(a, sl, fin, k);
+    else a.ctl[2] = 1u;
   }
 }
 
@@ -177,16 +200,12 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   __shared__ uint32_t bounds[2];
   const int64_t b0 = (int64_t)blockIdx.x * blockDim.x;
   const int64_t b1 = min(b0 + (int64_t)blockDim.x, a.n) - 1;
-  if (threadIdx.x == 0 || threadIdx.x == 32) {
-    const int64_t s = threadIdx.x == 0 ? b0 : b1;
+  const int wid = threadIdx.x >> 5;
+  if (wid < 2) {  // warp 0: the block's first slot, warp 1: its last
+    const int64_t s = wid == 0 ? b0 : b1;
     const unsigned long long vb = ((unsigned long long)a.keyA[s] << 32) | (uint32_t)s;
-    uint32_t lo = 0, hi = m;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (a.msorted[mid] < vb) lo = mid + 1;
-      else hi = mid;
-    }
-    bounds[threadIdx.x == 0 ? 0 : 1] = lo;
+    const uint32_t c = warp_count_below(a.msorted, 0, m, vb, threadIdx.x & 31);
+    if ((threadIdx.x & 31) == 0) bounds[wid] = c;
   }
   __syncthreads();
   if (i >= a.n || ((a.mask[i >> 5] >> (i & 31)) & 1u)) return;
@@ -199,12 +218,8 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
     else hi = mid;
   }
   const int64_t fin = i - (int64_t)movers_before(a, i, m) + lo;
-  if (fin >= 0 && fin < a.n) {
-    a.keyS[fin] = k;
-    a.perm[fin] = (uint32_t)i;
-  } else {
-    a.ctl[2] = 1u;
-  }
+  if (fin >= 0 && fin < a.n) place(a, i, fin, k);
+  else a.ctl[2] = 1u;
 }
 
 }  // namespace

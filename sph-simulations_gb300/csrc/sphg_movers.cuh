@@ -24,6 +24,14 @@ struct MoverArgs {
   uint32_t* perm;          // out: previous slot of each sorted position
   unsigned long long cond; // graph conditional handle of the full sort (0: none), set to
                            // 1 when it must run, 0 when the merge handled the iteration
+  // the merge scatters the state into sorted order itself (the reorder then only
+  // builds the cell ranges): sources in previous-slot order, destinations sorted
+  const float2* posB;
+  const float2* velB;
+  const int32_t* idsB;     // null when creation indices are not tracked
+  float2* posA;
+  float4* velpA;
+  int32_t* idsA;
 };
 
 int mover_groups(int64_t n);

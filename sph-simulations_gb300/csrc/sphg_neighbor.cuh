@@ -15,10 +15,15 @@
 namespace sphg {
 
 // Constants of the instance owning slot i (by value so they live in registers).
+// Batched: the instance of the first slot of i's 256-slot block from a table
+// built with the layout, then forward over the (rare) instance starts inside
+// the block -- instances hold at least hundreds of slots, so one or two loads.
 template <bool BATCHED>
 __device__ __forceinline__ InstDesc inst_of(const StepArgs& a, int64_t i) {
   if (!BATCHED) return a.d0;
-  return a.desc[find_instance(a.begins, a.ninst, (int)i)];
+  int k = __ldg(a.inst_tab + (i >> kInstTabShift));
+  while (k + 1 < a.ninst && __ldg(a.begins + k + 1) <= (int32_t)i) ++k;
+  return a.desc[k];
 }
 
 static __device__ __noinline__ int offset_cells_d(float o, double cs_d) {

@@ -123,7 +123,8 @@ void stage_newcomer(sphg_server* s, const SrvReq& r, const InstDesc& d, size_t a
   const sphg_sim* sim = s->sim;
   const int cmx = d.periodic ? d.nxr - 1 : d.nx - 1;
   const int cmy = d.periodic ? d.nyr - 1 : d.ny - 1;
-  for (int64_t i = 0; i < r.n; ++i) {
+  parallel_for(r.n, [&](int64_t b, int64_t e) {
+  for (int64_t i = b; i < e; ++i) {
     int cx, cy;
     float2 pos;
     if (sim->opt.precision == SPHG_PRECISION_SPLIT) {
@@ -142,6 +143,7 @@ void stage_newcomer(sphg_server* s, const SrvReq& r, const InstDesc& d, size_t a
     s->hkey[at + i] = d.order == 0 ? morton_host((uint32_t)cx, (uint32_t)cy) : (uint32_t)(cx + cy * d.nx);
     s->hids[at + i] = (int32_t)i;
   }
+  });
 }
 
 // Layout of a candidate live list (fails with SPHG_CAPACITY when it does not fit).
@@ -252,7 +254,8 @@ sphg_status retire(sphg_server* s, SrvReq& r, cudaStream_t st) {
   r.rvx.resize(n);
   r.rvy.resize(n);
   r.rrho.resize(n);
-  for (int64_t i = 0; i < n; ++i) {
+  parallel_for(n, [&](int64_t lo, int64_t hi) {
+  for (int64_t i = lo; i < hi; ++i) {
     double px = pos[i].x, py = pos[i].y;
     if (sim->opt.precision == SPHG_PRECISION_SPLIT) {
       int cx, cy;
@@ -268,6 +271,7 @@ sphg_status retire(sphg_server* s, SrvReq& r, cudaStream_t st) {
     r.rvy[i] = velp[i].y;
     r.rrho[i] = rho[i];
   }
+  });
   r.rids = ids;
   r.t_done = now_s(s->t0);
   r.state = 2;

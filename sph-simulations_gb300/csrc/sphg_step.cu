@@ -78,14 +78,15 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
 __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const uint32_t src = a.perm[i];
   const uint32_t k = a.keyS[i];
   a.keyA[i] = k;
-  float2 p = a.posB[src];
-  float2 v = a.velB[src];
-  a.posA[i] = p;
-  a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
-  if (a.track_ids) a.idsA[i] = a.idsB[src];
+  if (!(a.merged && *a.merged)) {  // gather (after a full sort; a merge scattered the state already)
+    const uint32_t src = a.perm[i];
+    a.posA[i] = a.posB[src];
+    const float2 v = a.velB[src];
+    a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
+    if (a.track_ids) a.idsA[i] = a.idsB[src];
+  }
   uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
   const uint32_t kprev = i > 0 ? a.keyS[i - 1] : kNoIndex;
   const uint32_t knext = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;

@@ -9,6 +9,8 @@
 namespace sphg {
 
 // Everything a step kernel touches.  Passed by value (kernel parameter space).
+constexpr int kInstTabShift = 8;  // slots per instance-table entry: 256
+
 struct StepArgs {
   int64_t n;
   int ninst;
@@ -17,6 +19,7 @@ struct StepArgs {
   InstDesc d0;                 // copy of desc[0] (single-instance fast path)
   const InstDesc* desc;        // [ninst]
   const int32_t* begins;       // [ninst]
+  const int32_t* inst_tab;     // [n >> kInstTabShift + 1] instance of the first slot of each block
   // sorted ("current") state
   float2* posA;
   float4* velpA;               // (vx, vy, p/rho^2, 1/rho)
@@ -38,6 +41,7 @@ struct StepArgs {
   int nbr_slots;
   const int64_t* csr_offs;     // [n+1] CSR neighbour lists of this iteration (lists mode)
   const uint32_t* csr_idx;     // j << 5 | tag entries, self included, list order
+  const uint32_t* merged;      // non-null and set: this iteration's merge scattered the state (reorder: ranges only)
   uint32_t* mover_mask;        // [ceil(n/32)] force pass: bit per slot whose key changed (or null)
   uint32_t* mover_gsum;        // [groups of 65,536 slots] changed slots per group (zeroed before)
   uint32_t* ghist;             // digit histograms of the next sort (accumulated by the key writers)
