@@ -26,6 +26,16 @@ __device__ __forceinline__ InstDesc inst_of(const StepArgs& a, int64_t i) {
   return a.desc[k];
 }
 
+// The same as a reference: batched kernels read each constant where it is used
+// (L1-cached) instead of holding the whole descriptor in registers.
+template <bool BATCHED>
+__device__ __forceinline__ const InstDesc& inst_ref(const StepArgs& a, int64_t i) {
+  if (!BATCHED) return a.d0;
+  int k = __ldg(a.inst_tab + (i >> kInstTabShift));
+  while (k + 1 < a.ninst && __ldg(a.begins + k + 1) <= (int32_t)i) ++k;
+  return a.desc[k];
+}
+
 static __device__ __noinline__ int offset_cells_d(float o, double cs_d) {
   return (int)floor(__ddiv_rn((double)o, cs_d));
 }
@@ -193,50 +203,6 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
     }
   }
   bool border = false;
-  if constexpr (!ORDERED) {
-    // One loop over the concatenated candidates of the non-empty cells (k
-    // ascending, j ascending: the same visiting order as cell by cell).  A warp
-    // runs max over lanes of the candidate total instead of the sum over cells
-    // of the per-cell maxima, which keeps more lanes busy per instruction.
-    uint32_t todo = 0;
-#pragma unroll
-    for (int q = 0; q < 9; ++q)
-      if (re[q] > rs[q]) todo |= 1u << q;
-    uint32_t j = 0, e = 0;
-    int k = 0;
-    float shx = 0.f, shy = 0.f;
-    bool wrapped = false;
-    while (true) {
-      if (j >= e) {
-        if (!todo) break;
-        k = __ffs(todo) - 1;
-        todo &= todo - 1;
-#pragma unroll
-        for (int q = 0; q < 9; ++q)
-          if (q == k) {
-            j = rs[q];
-            e = re[q];
-          }
-        if (PREC == 1) {
-          const int c1 = k / 3 - 1, c2 = k - 3 * (k / 3) - 1;
-          shx = c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x);
-          shy = c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y);
-        }
-        wrapped = (PREC == 0) && ((wrapmask >> k) & 1u);
-      }
-      const float2 pj = __ldg(pos + j);
-      float dx = (pi.x - pj.x) - shx;
-      float dy = (pi.y - pj.y) - shy;
-      if (wrapped) {
-        if (wrapped_pair(d, pi, pj, dx, dy)) visit(j, dx, dy, fmaf(dx, dx, dy * dy), (uint32_t)k | 16u);
-      } else {
-        const float r2 = fmaf(dx, dx, dy * dy);
-        if (r2 < d.h2_lo) visit(j, dx, dy, r2, (uint32_t)k);
-        else if (r2 <= d.h2_hi) border = true;
-      }
-      ++j;
-    }
-  } else {
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int c1 = k / 3 - 1, c2 = k % 3 - 1;
@@ -262,7 +228,6 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
       }
     };
     for (uint32_t j = rs[k]; j < re[k]; ++j) candidate(j, __ldg(pos + j));
-  }
   }
   if (ORDERED || !border) return;
 #pragma unroll 1

@@ -130,7 +130,7 @@ template <int PREC, bool BATCHED, bool CSR>
 __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const InstDesc d = inst_of<BATCHED>(a, i);
+  typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   typename std::conditional<PREC == 1, CSum, PSum>::type S;
@@ -193,8 +193,10 @@ template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
                                               uint32_t (*bj)[kThreads]);
 
+// Four blocks per SM (64 registers) for one instance, three for the batched
+// variants (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
+__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs a) {
   __shared__ float2 bd[kForceBuf][kThreads];
   __shared__ uint32_t bj[kForceBuf][kThreads];
   __shared__ uint32_t moved_in_block;
@@ -223,39 +225,44 @@ __global__ void __launch_bounds__(kThreads) step_force(StepArgs a) {
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
                                               uint32_t (*bj)[kThreads]) {
-  const InstDesc d = inst_of<BATCHED>(a, i);
+  // one instance: a copy of the kernel-argument descriptor; batched: a reference
+  typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   const float4 vi = a.velpA[i];
   typedef typename std::conditional<PREC == 1, CSum, PSum>::type Sum;
-  Sum fpx, fpy, fvx, fvy, fax, fay;
+  // one (compensated) sum per axis of every pair's pressure + viscosity (+ alpha) term
+  Sum fx, fy;
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
   const float alpha_c0 = d.alpha_c0;
+  const float rho_i = 1.0f / vi.w;
   const float4* __restrict__ velp = a.velpA;
   auto pair_v = [&](const float4 vj, float dx, float dy) {
     const float r2 = fmaf(dx, dx, dy * dy);
     const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
     const float r = r2 * rinv;
     const float hr = h - r;
-    if (r2 > tol2) {
-      const float s = kp * hr * hr * rinv * (vi.z + vj.z);
-      fpx.add(s * dx);
-      fpy.add(s * dy);
-    }
+    // viscosity (Laplacian): mu m / (rho_j pi h^6) 45 (h - r) (v_j - v_i)
     const float vm = kv * vj.w * hr;
-    fvx.add(vm * (vj.x - vi.x));
-    fvy.add(vm * (vj.y - vi.y));
-    if (alpha_c0 > 0.f && r2 > tol2) {
-      const float vr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy;
-      if (vr < 0.f) {
-        const float muij = h * vr / (r2 + d.eps_h2);
-        const float rho_bar = 0.5f * (1.0f / vi.w + 1.0f / vj.w);
-        const float pij = -alpha_c0 * muij / rho_bar;
-        const float s = d.ka * hr * hr * rinv * pij;
-        fax.add(s * dx);
-        fay.add(s * dy);
+    float tx = vm * (vj.x - vi.x);
+    float ty = vm * (vj.y - vi.y);
+    if (r2 > tol2) {
+      // pressure (spiky gradient, symmetric p / rho^2 form)
+      float s = kp * (vi.z + vj.z);
+      if (alpha_c0 > 0.f) {
+        const float vr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy;
+        if (vr < 0.f) {
+          // Monaghan: Pi_ij = -alpha c0 h vr / ((r^2 + eps h^2) rho_bar), rho_bar = (rho_i + rho_j) / 2
+          const float pij = -2.0f * alpha_c0 * h * vr * __fdividef(1.0f, (r2 + d.eps_h2) * (rho_i + 1.0f / vj.w));
+          s = fmaf(d.ka, pij, s);
+        }
       }
+      s *= hr * hr * rinv;
+      tx = fmaf(s, dx, tx);
+      ty = fmaf(s, dy, ty);
     }
+    fx.add(tx);
+    fy.add(ty);
   };
   auto pair = [&](uint32_t j, float dx, float dy) { pair_v(__ldg(velp + j), dx, dy); };
   int cx, cy;
@@ -321,14 +328,8 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
       pair(bj[q][t], dd.x, dd.y);
     }
   }
-  float ax = d.gx + fpx.value();
-  float ay = d.gy + fpy.value();
-  ax += fvx.value();
-  ay += fvy.value();
-  if (alpha_c0 > 0.f) {
-    ax += fax.value();
-    ay += fay.value();
-  }
+  const float ax = d.gx + fx.value();
+  const float ay = d.gy + fy.value();
   if (MODE == kForceOnly) {
     a.acc[i] = make_float2(ax, ay);
     return 0;
