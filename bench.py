@@ -18,8 +18,8 @@ One "step" is one main-loop iteration of the reference
 `value` is device time with the state resident in HBM (CUDA events on the
 launching stream, L2 flushed by a 256 MiB write between timed steps); `e2e` is
 the same run driven through the C ABI from host buffers (upload, pre-loop, K
-iterations each followed by the step-header diagnostics read back, final
-download), timed on the host around the whole sequence.
+iterations each followed by its step-header diagnostics copied into pinned host
+memory, final download), timed on the host around the whole sequence.
 
 --impl reference times the reference algorithm on the host cores: the CPU
 restatement of the reference's OpenMP path (oracle/liboracle.so, FP64, all
@@ -310,22 +310,29 @@ def run_gpu(args):
                                     "how": "one handle per instance, stepped in turn"},
                  "batched_vs_plain": value / plain}
 
-    # ---- end to end through the C ABI from host buffers
+    # ---- end to end through the C ABI from host buffers: upload of the initial
+    #      state, pre-loop, every step followed by its step header (E_k, max|v|^2,
+    #      N inside, momentum) copied into pinned host memory, final download
     sim = sphg.Sim(sprm, w["counts"] if batched else n, opts)
+    ninst = len(prm) if batched else 1
+    headers = torch.empty((args.steps, 6 * ninst), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.upload(x, y, vx, vy, stream=sptr)
     sim.preloop(stream=sptr)
     for k in range(args.steps):
         sim.step(1, stream=sptr)
-        sim.diagnostics(stream=sptr)  # the per-step header (E_k, max|v|^2, N) read back
-    out = sim.download(forces=False, stream=sptr)
+        sim.diagnostics_async(headers[k].data_ptr(), stream=sptr)
+    out = sim.download(forces=False, stream=sptr)  # synchronises; checks the device error words
     e2e_s = time.perf_counter() - t0
     sim.close()
-    ninst = len(prm) if batched else 1
+    hdr = headers.numpy()
+    assert np.isfinite(hdr).all() and (hdr[:, 2::6].sum(axis=1) == n).all()
+    state_h2d = 8 + 8 + (4 if prec == sphg.SPLIT else 0)      # pos (or offset), vel, split cell key
+    state_d2h = 8 + 16 + 4 + (4 if prec == sphg.SPLIT else 0)  # pos, (v, p, 1/rho), rho, split cell key
     e2e = {"value": n * args.steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(n * 16 / args.steps),
-           "d2h_bytes_per_step": int(6 * 8 * ninst + n * (2 * 8 + 4 + 4 + 4) / args.steps),
+           "h2d_bytes_per_step": int(n * state_h2d / args.steps),
+           "d2h_bytes_per_step": int(6 * 8 * ninst + n * state_d2h / args.steps),
            "wall_s": e2e_s}
     assert np.isfinite(out["x"]).all()
 

@@ -158,6 +158,10 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
 /* Per instance, 6 doubles: E_k, max |v|^2, particles inside the domain,
  * sum m vx, sum m vy, non-finite count.  out has 6*ninst entries. */
 sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream);
+/* The same without waiting: the values land in out (pinned host memory, kept
+ * valid until the stream passes this point) in stream order, so a step loop
+ * reads every step's header without a host synchronisation per step. */
+sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream);
 
 /* Adaptive time step per instance from the current state: FP64 maxima of the
  * speed and of the acceleration on the device, then

@@ -885,6 +885,18 @@ sphg_status sphg_set_dt(sphg_sim* s, int32_t inst, double dt) {
   return SPHG_OK;
 }
 
+sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream) {
+  if (!s || !out) return fail(SPHG_INVALID_ARG, "null argument");
+  if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t max_n = 0;
+  for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
+  const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, s->diag_out, st));
+  SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst, cudaMemcpyDeviceToHost, st));
+  return SPHG_OK;
+}
+
 sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream) {
   if (!s || !host) return fail(SPHG_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;

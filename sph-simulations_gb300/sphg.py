@@ -115,6 +115,8 @@ def lib():
         L.sphg_delta_decode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
         L.sphg_autotune.argtypes = [ctypes.c_int32, PP, _lp, _dp, _dp, _dp, _dp, OP, ctypes.c_int32, OP,
                                     _dp, _vp]
+        L.sphg_diagnostics_async.argtypes = [SP, _vp, _vp]
+        L.sphg_diagnostics_async.restype = ctypes.c_int
         L.sphg_upload_lattice.argtypes = [SP, ctypes.POINTER(Lattice), _vp]
         L.sphg_upload_lattice.restype = ctypes.c_int
         L.sphg_cfl_dt.argtypes = [SP, ctypes.c_double, ctypes.c_double, _dp, _vp]
@@ -272,6 +274,10 @@ class Sim:
         check(lib().sphg_neighbor_lists_encoded(self._h, _ptr(offs, _lp), _ptr(enc, _ip),
                                                 ctypes.byref(total), _stream(stream)))
         return offs, enc[:total.value]
+
+    def diagnostics_async(self, out_ptr, stream=None):
+        """Enqueues the step header into pinned host memory at out_ptr (6 doubles per instance)."""
+        check(lib().sphg_diagnostics_async(self._h, out_ptr, _stream(stream)))
 
     def cfl_dt(self, cfl=0.25, force_coef=0.25, stream=None):
         out = np.zeros(self.ninst, np.float64)
