@@ -126,8 +126,9 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
   }
 }
 
+// Five blocks per SM (51 registers) for one instance.
 template <int PREC, bool BATCHED, bool CSR>
-__global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
+__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 5) step_density(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
@@ -371,6 +372,14 @@ __device__ __forceinline__ void block_reduce6(double (&v)[6], double (*sh)[kDiag
   __syncthreads();
 }
 
+// Per (chunk, instance) block.  The conservation sums (kinetic energy,
+// momentum) and max |v|^2 are FP64 from the FP32 velocities (products exact);
+// the in-domain count is decided in FP32 and redone in FP64 (out of line)
+// only within a thin band of a wall; counts are integers.
+static __device__ __noinline__ bool inside_d(double x, double y, const InstDesc& d) {
+  return !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd);
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, int chunks,
                                                                   double* partials) {
@@ -380,28 +389,41 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
   const int64_t per = (cnt + chunks - 1) / chunks;
   const int64_t b = d.begin + per * blockIdx.x;
   const int64_t e = min((int64_t)d.end, b + per);
-  double v[6] = {0, 0, 0, 0, 0, 0};  // E_k, max |v|^2, inside, sum m vx, sum m vy, non-finite
+  double ek = 0.0, px = 0.0, py = 0.0, vmax = 0.0;
+  int inside = 0, bad = 0;
+  const float band = 1.0e-6f * fmaxf(fabsf(d.hi_x - d.lo_x), fabsf(d.hi_y - d.lo_y));
   for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const float4 vel = a.velpA[i];
     const float2 p = a.posA[i];
     const double vx = vel.x, vy = vel.y;
     const double n2 = vx * vx + vy * vy;
-    v[0] += 0.5 * n2 * d.mass_d;
-    v[1] = fmax(v[1], n2);
-    v[3] += d.mass_d * vx;
-    v[4] += d.mass_d * vy;
-    double x = p.x, y = p.y;
+    ek += n2;
+    vmax = fmax(vmax, n2);
+    px += vx;
+    py += vy;
+    int cx = 0, cy = 0;
+    float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
+    float lox = d.lo_x, hix = d.hi_x, loy = d.lo_y, hiy = d.hi_y;
     if (PREC == 1) {
-      int cx, cy;
       decode_code(d, a.keyA[i] - d.cell_base, cx, cy);
-      x = d.lo_xd + cx * d.cs_xd + x;
-      y = d.lo_yd + cy * d.cs_yd + y;
+      lox = -(float)cx * d.cs_x;  // the walls in the cell's frame
+      hix = d.Lx - (float)cx * d.cs_x;
+      loy = -(float)cy * d.cs_y;
+      hiy = d.Ly - (float)cy * d.cs_y;
     }
-    const bool fin = isfinite(x) && isfinite(y) && isfinite(vx) && isfinite(vy) &&
-                     isfinite(a.rho[i]);
-    v[2] += (fin && !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd)) ? 1.0 : 0.0;
-    v[5] += fin ? 0.0 : 1.0;
+    const bool fin = isfinite(x) && isfinite(y) && isfinite(vel.x) && isfinite(vel.y) && isfinite(a.rho[i]);
+    bool in = fin && x >= lox && x <= hix && y >= loy && y <= hiy;
+    const bool near = fin && (fabsf(x - lox) <= band || fabsf(x - hix) <= band || fabsf(y - loy) <= band ||
+                              fabsf(y - hiy) <= band);
+    if (near) {
+      const double xd = PREC == 1 ? d.lo_xd + cx * d.cs_xd + (double)x : (double)x;
+      const double yd = PREC == 1 ? d.lo_yd + cy * d.cs_yd + (double)y : (double)y;
+      in = inside_d(xd, yd, d);
+    }
+    inside += in ? 1 : 0;
+    bad += fin ? 0 : 1;
   }
+  double v[6] = {0.5 * d.mass_d * ek, vmax, (double)inside, d.mass_d * px, d.mass_d * py, (double)bad};
   __shared__ double sh[6][kDiagThreads / 32];
   block_reduce6(v, sh);
   if (threadIdx.x < 6) partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = sh[threadIdx.x][0];
