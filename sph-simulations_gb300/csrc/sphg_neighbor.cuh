@@ -203,45 +203,6 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
     }
   }
   bool border = false;
-  if (!ORDERED && !d.periodic && d.order == 0) {
-    // Morton, walls: the two cells of a stencil row that share cx >> 1 have
-    // consecutive codes, so their particles are adjacent in the sorted order --
-    // one loop covers both (the cell of a candidate is read off the split
-    // point).  Six loops per particle instead of nine; rows are visited in turn
-    // (a different but fixed summation order).
-    const bool even = (cx & 1) == 0;
-    const int ca = even ? 0 : -1;  // x offset of the pair's first cell (the second is ca + 1)
-    const int cs1 = even ? -1 : 1;  // x offset of the row's third cell
-    const float shA = (PREC == 1) ? (ca == 0 ? 0.f : -d.cs_x) : 0.f;
-    const float shB = (PREC == 1) ? (ca == 0 ? d.cs_x : 0.f) : 0.f;
-    const float shS = (PREC == 1) ? (cs1 > 0 ? d.cs_x : -d.cs_x) : 0.f;
-#pragma unroll
-    for (int c2 = -1; c2 <= 1; ++c2) {
-      const int kL = c2 + 1, kC = 3 + c2 + 1, kR = 6 + c2 + 1;
-      const uint32_t sA = even ? rs[kC] : rs[kL], eA = even ? re[kC] : re[kL];
-      const uint32_t sB = even ? rs[kR] : rs[kC], eB = even ? re[kR] : re[kC];
-      const uint32_t sS = even ? rs[kL] : rs[kR], eS = even ? re[kL] : re[kR];
-      const bool hasA = eA > sA, hasB = eB > sB;
-      const uint32_t s0 = hasA ? sA : (hasB ? sB : 0u);
-      const uint32_t e0 = hasB ? eB : (hasA ? eA : 0u);
-      const uint32_t split = hasA ? eA : s0;
-      const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
-      const uint32_t tagA = (uint32_t)(3 * (ca + 1) + (c2 + 1)), tagB = tagA + 3u;
-      const uint32_t tagS = (uint32_t)(3 * (cs1 + 1) + (c2 + 1));
-      auto candidate = [&](uint32_t j, float2 pj, float shx, uint32_t tag) {
-        const float dx = (pi.x - pj.x) - shx;
-        const float dy = (pi.y - pj.y) - shy;
-        const float r2 = fmaf(dx, dx, dy * dy);
-        if (r2 < d.h2_lo) visit(j, dx, dy, r2, tag);
-        else if (r2 <= d.h2_hi) border = true;
-      };
-      for (uint32_t j = s0; j < e0; ++j) {
-        const bool inA = j < split;
-        candidate(j, __ldg(pos + j), inA ? shA : shB, inA ? tagA : tagB);
-      }
-      for (uint32_t j = sS; j < eS; ++j) candidate(j, __ldg(pos + j), shS, tagS);
-    }
-  } else {
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int c1 = k / 3 - 1, c2 = k % 3 - 1;
@@ -267,7 +228,6 @@ __device__ __forceinline__ void for_each_neighbor(const StepArgs& a, const InstD
       }
     };
     for (uint32_t j = rs[k]; j < re[k]; ++j) candidate(j, __ldg(pos + j));
-  }
   }
   if (ORDERED || !border) return;
 #pragma unroll 1

@@ -126,9 +126,8 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
   }
 }
 
-// Five blocks per SM (51 registers) for one instance.
 template <int PREC, bool BATCHED, bool CSR>
-__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 5) step_density(StepArgs a) {
+__global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);

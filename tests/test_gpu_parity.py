@@ -397,8 +397,11 @@ def test_tiled_kernels_match_oracle_and_untiled(prec, tb):
         sim.close()
     a, b = res[tb][0], res[-1][0]
     assert (a["ids"] == b["ids"]).all()
+    # both within ACC_TOL of the oracle, in different summation orders: velocities
+    # agree to 3 steps x dt x 2 ACC_TOL x max|a|
+    amax = max(np.abs(b["fx"]).max(), np.abs(b["fy"]).max())
     for k in ("x", "y", "vx", "vy"):
-        np.testing.assert_allclose(a[k], b[k], rtol=1e-6, atol=1e-9)
+        np.testing.assert_allclose(a[k], b[k], rtol=1e-6, atol=max(1e-9, 3 * 1e-5 * 2 * ACC_TOL * amax * 2))
     np.testing.assert_allclose(a["rho"], b["rho"], rtol=1e-6)
 
 
