@@ -152,13 +152,16 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
     const uint32_t slots = (uint32_t)a.nbr_slots;
     const size_t n = (size_t)a.n;
     uint32_t cnt = 0;
-    for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
-      float t = fmaf(-r2, inv_h2, 1.0f);
+    auto accept = [&](uint32_t e, float r2) {  // e = j << 5 | stencil tag
+      const float t = fmaf(-r2, inv_h2, 1.0f);
       S.add(t * t * t);
-      if (nbr && j != (uint32_t)i) {  // record the pair for the force pass
-        if (cnt < slots) nbr[cnt * n + i] = (j << 5) | tag;
+      if (nbr && (e >> 5) != (uint32_t)i) {  // record the pair for the force pass
+        if (cnt < slots) nbr[cnt * n + i] = e;
         ++cnt;
       }
+    };
+    for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
+      accept((j << 5) | tag, r2);
     });
     if (nbr) a.ncount[i] = cnt;
   }

@@ -846,3 +846,21 @@ def test_device_taylor_green_lattice():
     with pytest.raises(S.SphgError):
         sim.upload_lattice(S.lattice(0, 0, 0.1, 0.1, 10, 10))  # 100 != 1024 particles
     sim.close()
+
+
+def test_diagnostics_async_equals_sync():
+    import torch
+    S = _sphg()
+    x, y, vx, vy = jittered(40, 40, 0.005, seed=23, vel=0.3)
+    sim = S.Sim(S.params(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.3, 0.3)), len(x))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    buf = torch.zeros((5, 6), dtype=torch.float64, pin_memory=True)
+    sync = []
+    for k in range(5):
+        sim.step(2)
+        sim.diagnostics_async(buf[k].data_ptr())
+        torch.cuda.synchronize()
+        sync.append(sim.diagnostics()[0])
+    assert (buf.numpy() == np.array(sync)).all()
+    sim.close()
