@@ -145,4 +145,28 @@ __device__ __forceinline__ int find_instance(const int32_t* __restrict__ begins,
   return lo;
 }
 
+// Launch with programmatic dependent launch: the kernel may be scheduled while
+// the previous kernel in the stream finishes; it must call
+// cudaGridDependencySynchronize() before touching that kernel's results (a
+// no-op when launched without the attribute).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+#ifdef SPHG_NO_PDL
+  cfg.numAttrs = 0;
+#else
+  cfg.numAttrs = 1;
+#endif
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace sphg

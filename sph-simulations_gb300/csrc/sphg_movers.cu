@@ -23,6 +23,7 @@
 
 #include <cuda_runtime.h>
 
+#include "sphg_common.cuh"
 #include "sphg_movers.cuh"
 
 namespace sphg {
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
 // 32-way search of the slots' (key, slot) order (four or five dependent
 // rounds instead of twenty for a million slots).
 __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
+  cudaGridDependencySynchronize();  // the mover list and decision of movers_compact
   if (!a.ctl[0]) return;
   const uint32_t m = a.ctl[1];
   const int lane = threadIdx.x & 31;
@@ -191,6 +193,7 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
 
 // Thread i places slot i if it kept its key (the movers are placed already).
 __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
+  cudaGridDependencySynchronize();  // the sorted movers of movers_rank_place
   if (!a.ctl[0]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m = a.ctl[1];
@@ -231,8 +234,12 @@ cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
   const int64_t cap = a.n < kMoverCap ? a.n : kMoverCap;
   const int per_block = kRankThreads / 32;
   movers_compact<<<mover_groups(a.n), kCompactThreads, 0, st>>>(a);
-  movers_rank_place<<<(unsigned)((cap + per_block - 1) / per_block), kRankThreads, 0, st>>>(a);
-  movers_merge<<<(unsigned)((a.n + kStayThreads - 1) / kStayThreads), kStayThreads, 0, st>>>(a);
+  cudaError_t e = launch_pdl(movers_rank_place, dim3((unsigned)((cap + per_block - 1) / per_block)),
+                             dim3(kRankThreads), 0, st, a);
+  if (e != cudaSuccess) return e;
+  e = launch_pdl(movers_merge, dim3((unsigned)((a.n + kStayThreads - 1) / kStayThreads)), dim3(kStayThreads), 0,
+                 st, a);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

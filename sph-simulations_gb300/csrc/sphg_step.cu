@@ -128,6 +128,7 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
 
 template <int PREC, bool BATCHED, bool CSR>
 __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
+  cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
@@ -200,6 +201,7 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
 // variants (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs a) {
+  cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
   __shared__ float2 bd[kForceBuf][kThreads];
   __shared__ uint32_t bj[kForceBuf][kThreads];
   __shared__ uint32_t moved_in_block;
@@ -516,6 +518,21 @@ static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t -
     }                                                                     \
   } while (0)
 
+// The same with programmatic dependent launch (the kernel synchronises on its
+// predecessor's grid itself).
+#define SPHG_DISPATCH2_PDL(PREC_RT, BATCH_RT, KERNEL, ...)                                   \
+  do {                                                                                      \
+    cudaError_t e_ = cudaSuccess;                                                           \
+    if (PREC_RT) {                                                                          \
+      if (BATCH_RT) e_ = launch_pdl(KERNEL<1, true __VA_ARGS__>, dim3(g), dim3(kThreads), 0, s, a);  \
+      else e_ = launch_pdl(KERNEL<1, false __VA_ARGS__>, dim3(g), dim3(kThreads), 0, s, a);          \
+    } else {                                                                                \
+      if (BATCH_RT) e_ = launch_pdl(KERNEL<0, true __VA_ARGS__>, dim3(g), dim3(kThreads), 0, s, a);  \
+      else e_ = launch_pdl(KERNEL<0, false __VA_ARGS__>, dim3(g), dim3(kThreads), 0, s, a);          \
+    }                                                                                       \
+    if (e_ != cudaSuccess) return e_;                                                       \
+  } while (0)
+
 cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const unsigned g = blocks_for(a.n, kThreads);
@@ -534,7 +551,7 @@ cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s, boo
   const unsigned g = blocks_for(a.n, kThreads);
   const bool b = (a.ninst > 1 || a.force_batched);
   if (csr) SPHG_DISPATCH2(precision, b, step_density, , true);
-  else SPHG_DISPATCH2(precision, b, step_density, , false);
+  else SPHG_DISPATCH2_PDL(precision, b, step_density, , false);
   return cudaGetLastError();
 }
 
@@ -547,7 +564,7 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
     else SPHG_DISPATCH2(precision, b, step_force, , kForceIntegrate, true);
   } else {
     if (mode == kForceOnly) SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, false);
-    else SPHG_DISPATCH2(precision, b, step_force, , kForceIntegrate, false);
+    else SPHG_DISPATCH2_PDL(precision, b, step_force, , kForceIntegrate, false);
   }
   return cudaGetLastError();
 }
