@@ -864,3 +864,32 @@ def test_diagnostics_async_equals_sync():
         sync.append(sim.diagnostics()[0])
     assert (buf.numpy() == np.array(sync)).all()
     sim.close()
+
+
+@pytest.mark.parametrize("prec", ["plain", "split"])
+def test_particles_outside_the_high_walls(prec):
+    """Particles beyond the high walls at upload: their cells clamp to the last
+    cell (GenericNeighborSearch::SetParticleCellIds clamps ci <= n - 1) and the
+    first integration puts them on the walls with reflected velocity
+    (Integrator::ApplyBoundaryConditions)."""
+    S = _sphg()
+    x, y, vx, vy = jittered(30, 30, 0.005, seed=29, vel=0.2)
+    x[:5] = 0.3 + np.array([1e-4, 2e-3, 5e-3, 0.0, 3e-4])  # hi = 0.3
+    y[5:10] = 0.3 + np.array([1e-4, 2e-3, 5e-3, 0.0, 3e-4])
+    x = x.astype(np.float32).astype(np.float64)
+    y = y.astype(np.float32).astype(np.float64)
+    kw = dict(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.3, 0.3))
+    p = O.params(**kw)
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    sim = S.Sim(S.params(**kw), len(x), S.options(precision=P))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    a = sim.download()
+    sk, s, e, rho, fx, fy = oracle_state(p, a)
+    assert (sim.debug(S.DBG_KEYS) == sk).all()
+    assert rel_rho(a["rho"], rho) <= RHO_TOL
+    nx_, ny_ = sim.debug(S.DBG_POS_NEXT)
+    ox, oy, _, _ = O.integrate(p, a["x"], a["y"], a["vx"], a["vy"], a["fx"], a["fy"])
+    assert np.max(np.abs(nx_ - ox)) < 1e-7 and np.max(np.abs(ny_ - oy)) < 1e-7
+    assert (nx_ <= 0.3 + 1e-7).all() and (ny_ <= 0.3 + 1e-7).all()  # on the walls, within FP32 rounding
+    sim.close()
