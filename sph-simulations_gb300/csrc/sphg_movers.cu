@@ -197,24 +197,22 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   if (!a.ctl[0]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m = a.ctl[1];
-  // a stayer: its rank among stayers + the movers ordered before it.  The
-  // block's slots are consecutive, so the movers ordered before any of them lie
-  // between the counts of its first and last slot (two searches per block).
-  __shared__ uint32_t bounds[2];
-  const int64_t b0 = (int64_t)blockIdx.x * blockDim.x;
-  const int64_t b1 = min(b0 + (int64_t)blockDim.x, a.n) - 1;
-  const int wid = threadIdx.x >> 5;
-  if (wid < 2) {  // warp 0: the block's first slot, warp 1: its last
-    const int64_t s = wid == 0 ? b0 : b1;
-    const unsigned long long vb = ((unsigned long long)a.keyA[s] << 32) | (uint32_t)s;
-    const uint32_t c = warp_count_below(a.msorted, 0, m, vb, threadIdx.x & 31);
-    if ((threadIdx.x & 31) == 0) bounds[wid] = c;
-  }
-  __syncthreads();
+  // a stayer: its rank among stayers + the movers ordered before it.  A warp's
+  // slots are consecutive, so the movers ordered before any of them lie
+  // between the counts of its first and last slot: two warp-wide searches per
+  // warp, then each lane refines inside that (usually empty) interval.
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = i - lane;
+  if (w0 >= a.n) return;  // the whole warp is past the last slot
+  const int64_t w1 = min(w0 + 31, a.n - 1);
+  const unsigned long long v0 = ((unsigned long long)a.keyA[w0] << 32) | (uint32_t)w0;
+  const unsigned long long v1 = ((unsigned long long)a.keyA[w1] << 32) | (uint32_t)w1;
+  const uint32_t wlo = warp_count_below(a.msorted, 0, m, v0, lane);
+  const uint32_t whi = warp_count_below(a.msorted, wlo, m, v1, lane);
   if (i >= a.n || ((a.mask[i >> 5] >> (i & 31)) & 1u)) return;
   const uint32_t k = a.keyA[i];
   const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
-  uint32_t lo = bounds[0], hi = bounds[1];
+  uint32_t lo = wlo, hi = whi;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
     if (a.msorted[mid] < v) lo = mid + 1;
