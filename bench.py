@@ -438,6 +438,7 @@ def run_serve(args):
                    "capacity_particles": st["cap_particles"], "capacity_cell_keys": st["cap_keys"]},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max()), "mean": float(lat.mean())},
+        "offered_particle_steps_per_s": sum(len(r[3]) * r[7] for r in reqs) / args.serve_seconds,
         "wall_s": wall, "ticks": st["ticks"], "device_particle_steps": st["particle_steps"],
         "clocks": clk,
     }

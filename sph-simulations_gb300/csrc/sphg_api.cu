@@ -670,6 +670,12 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
     return st;
   }
   st = apply_layout(s, ninst, p, counts, L, nullptr);
+  // set-up that would otherwise land on the first upload / step: the pinned
+  // staging of upload and download, and the captured graph of an iteration
+  if (st == SPHG_OK && s->n > 0 &&
+      !host_stage(s, (size_t)s->n * (sizeof(float2) * 2 + sizeof(float4) + sizeof(float) + sizeof(uint32_t))))
+    st = fail(SPHG_OOM, "pinned host staging");
+  if (st == SPHG_OK && s->n > 0 && s->opt.use_graph) st = build_graph(s);
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;
