@@ -66,13 +66,13 @@ def peaks():
 import workloads as W  # noqa: E402  (sph-simulations_gb300/workloads.py)
 
 WORKLOADS = {
-    # configs[1]: 1,000,000-particle dam break, split-precision positions (the headline)
+    # 1,000,000-particle dam break, split-precision positions (the headline)
     "dam_break_1m": dict(kind="dam", nx=1000, ny=1000, dx=0.0005, steps_config=2000, precision="split"),
-    # configs[0]: 12,800-particle dam break, plain FP32 positions
+    # 12,800-particle dam break, plain FP32 positions
     "dam_break_12k": dict(kind="dam", nx=80, ny=160, dx=0.005, steps_config=1000, precision="plain"),
-    # configs[2]: periodic Taylor-Green vortex, 512 x 512
+    # periodic Taylor-Green vortex, 512 x 512
     "tgv_262k": dict(kind="tgv", n=512, steps_config=5000, precision="plain"),
-    # configs[3]: 256 independent dam-break boxes, 2,000-65,536 particles each
+    # 256 independent dam-break boxes, 2,000-65,536 particles each
     "batch_256": dict(kind="batch", count=256, steps_config=1000, precision="split"),
 }
 
@@ -386,7 +386,7 @@ def run_gpu(args):
 
 
 def run_serve(args):
-    """configs[4]: Poisson arrivals (200/s by default) of dam-break / Taylor-Green
+    """Serving: Poisson arrivals (200/s by default) of dam-break / Taylor-Green
     requests (50/50), 1e3-2e5 particles, 500 steps each, admitted by a fixed HBM
     budget into one continuously batched server; requests are generated before
     the clock starts and submitted at their arrival times."""

@@ -252,10 +252,8 @@ sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond
 // The full stable radix sort of the next keys (skip: device word that makes
 // its kernels return at once, or null).
 sphg_status enqueue_full_sort(sphg_sim* s, cudaStream_t st, const uint32_t* skip) {
-  const StepArgs a = s->args();
   SPHG_CUDA(sphg::radix_sort_pairs(s->keyB, nullptr, s->keyTmp, s->perm, s->keyA, s->valTmp,
-                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, a.ghist, skip));
-  if (a.ghist) SPHG_CUDA(cudaMemsetAsync(a.ghist, 0, sizeof(uint32_t) * 4 * 256, st));
+                                   s->scratch, s->n, s->key_bits, st, s->flags + 2, nullptr, skip));
   return SPHG_OK;
 }
 

@@ -118,8 +118,6 @@ struct sphg_sim {
     a.tile_count = flags + 1;
     a.force_batched = force_batched;
     a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
-    a.ghist = nullptr;  // the sort computes its digit histograms itself
-    a.key_passes = (key_bits + 7) / 8;
     a.ncount = ncount;
     a.nbr_slots = nbr_slots;
     a.csr_offs = csr_offs;

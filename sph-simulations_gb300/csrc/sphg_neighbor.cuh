@@ -322,21 +322,4 @@ __device__ __forceinline__ uint32_t integrate_and_key(const StepArgs& a, const I
   return key;
 }
 
-// Adds one key per thread (valid == false: none) to the radix digit histograms
-// of the next sort: block-level counts in shared memory, then one global atomic
-// per (pass, digit).  Call with the whole block.
-__device__ __forceinline__ void histogram_keys(const StepArgs& a, uint32_t (*hs)[256], bool valid,
-                                               uint32_t key) {
-  const int lane = threadIdx.x & 31;
-  for (int p = 0; p < a.key_passes; ++p) {
-    const uint32_t dg = valid ? (key >> (8 * p)) & 255u : 256u;
-    const unsigned peers = __match_any_sync(0xffffffffu, dg);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&hs[p][dg], (uint32_t)__popc(peers));
-  }
-  __syncthreads();
-  for (int p = 0; p < a.key_passes; ++p)
-    for (int t = threadIdx.x; t < 256; t += blockDim.x)
-      if (hs[p][t]) atomicAdd(&a.ghist[p * 256 + t], hs[p][t]);
-}
-
 }  // namespace sphg

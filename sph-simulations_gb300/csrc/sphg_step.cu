@@ -32,9 +32,6 @@ constexpr int kThreads = 256;
 // ---------------------------------------------------------------- keys
 template <int PREC, bool BATCHED>
 __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
-  __shared__ uint32_t hs[4][256];
-  for (int p = 0; p < 4; ++p) hs[p][threadIdx.x] = 0;
-  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   uint32_t key = 0;
@@ -71,7 +68,6 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
     key = d.cell_base + local_code(d, cx, cy);
     a.keyB[i] = key;
   }
-  if (a.ghist) histogram_keys(a, hs, valid, key);
 }
 
 // ---------------------------------------------------------------- reorder + cell ranges

@@ -44,8 +44,6 @@ struct StepArgs {
   const uint32_t* merged;      // non-null and set: this iteration's merge scattered the state (reorder: ranges only)
   uint32_t* mover_mask;        // [ceil(n/32)] force pass: bit per slot whose key changed (or null)
   uint32_t* mover_gsum;        // [groups of 65,536 slots] changed slots per group (zeroed before)
-  uint32_t* ghist;             // digit histograms of the next sort (accumulated by the key writers)
-  int key_passes;              // radix passes of the next sort
   uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
   // cell tiles (Morton order only; tile_bits == 0 disables them)
   int tile_bits;               // tiles of 2^tile_bits x 2^tile_bits cells

@@ -8,13 +8,12 @@ gravity -9.81, artificial viscosity alpha, periodic boundaries, particle mass)
 are the library's extensions.
 
   dam_break(nx, ny, dx)   water column of nx x ny particles at the left wall of
-                          a box (configs 0 and 1; the 12,800 and 1,000,000
-                          particle cases)
-  taylor_green(n)         periodic Taylor-Green vortex on [0,1]^2 (config 2)
+                          a box (the 12,800- and 1,000,000-particle cases)
+  taylor_green(n)         periodic Taylor-Green vortex on [0,1]^2 (512 x 512)
   batch(count)            independent dam-break boxes of log-uniform sizes
-                          (config 3)
+                          (256 boxes of 2,000-65,536 particles)
   requests(rate, seconds) a Poisson stream of dam-break / Taylor-Green jobs
-                          (config 4)
+                          (200 per second, 1,000-200,000 particles)
 """
 import math
 
@@ -99,7 +98,7 @@ def taylor_green(n, seed=0, nu=0.01, order="morton", dt=2e-5):
 
 def dam_break_sized(npart, aspect, dx, rng, alpha, order="morton"):
     """A dam-break instance of about npart particles, column height/width = aspect,
-    box 2.5x the column width and 1.25x its height (the config-0 proportions)."""
+    box 2.5x the column width and 1.25x its height (the proportions of the 12,800-particle case)."""
     nx = max(2, int(round(math.sqrt(npart / aspect))))
     ny = max(2, int(round(npart / nx)))
     x, y = _jittered(nx, ny, dx, rng)

@@ -74,7 +74,7 @@ def default_rowmajor():
     np.savez_compressed(os.path.join(HERE, "default_rowmajor.npz"), **out)
 
 
-def cfg0_morton():
+def dam12k_morton():
     # dam-break column geometry of the 12,800-particle case: 80 x 160 lattice,
     # dx = 0.005 from (dx/2, dx/2), +-0.01 dx jitter, h = 1.3 dx, box [0,1]^2.
     dx = 0.005
@@ -91,7 +91,7 @@ def cfg0_morton():
     R.pressure_forces()
     a = R.get()
     key_in = O.cell_ids(p, x, y)
-    np.savez_compressed(os.path.join(HERE, "cfg0_morton.npz"), x_in=x, y_in=y, vx_in=vx,
+    np.savez_compressed(os.path.join(HERE, "dam12k_morton.npz"), x_in=x, y_in=y, vx_in=vx,
                         vy_in=vy, key_in=key_in, perm=perm, key=a["key"], rho=a["rho"],
                         fx=a["fx"], fy=a["fy"], h=p.h, dt=p.dt)
 
@@ -191,7 +191,7 @@ def main():
     assert O.ref_lib() is not None, "reference harness not built (needs the reference sources)"
     morton_kat()
     default_rowmajor()
-    cfg0_morton()
+    dam12k_morton()
     small_multistep()
     lists()
     tiny()

@@ -104,12 +104,12 @@ def test_sort_pairs_stable(n, bits):
 
 
 # ---------------------------------------------------------------- whole step vs reference goldens
-def test_preloop_matches_reference_cfg0(golden):
+def test_preloop_matches_reference_dam12k(golden):
     """12,800-particle dam-break geometry, reference physics (k=30, rho0=25, mu=0.01,
     g=-10, m=1), h = 0.0065, Morton: keys, cell membership, density and forces
     against the reference's own FP64 output."""
     S = _sphg()
-    g = golden("cfg0_morton")
+    g = golden("dam12k_morton")
     kw = dict(order="morton", h=float(g["h"]), dt=float(g["dt"]), lo=(0, 0), hi=(1, 1))
     sim = S.Sim(S.params(**kw), len(g["x_in"]))
     sim.upload(g["x_in"], g["y_in"], g["vx_in"], g["vy_in"])

@@ -59,8 +59,8 @@ def test_default_config_rowmajor(golden):
     np.testing.assert_allclose(d[:3], g["s2_diag"], rtol=1e-12)
 
 
-def test_cfg0_teacher_forced(golden):
-    g = golden("cfg0_morton")
+def test_dam12k_teacher_forced(golden):
+    g = golden("dam12k_morton")
     p = O.params(order="morton", h=float(g["h"]), dt=float(g["dt"]), lo=(0, 0), hi=(1, 1))
     key, perm, sk, s, e = O.find_neighbors(p, g["x_in"], g["y_in"])
     assert (key == g["key_in"]).all()
