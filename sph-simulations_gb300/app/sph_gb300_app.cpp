@@ -22,7 +22,10 @@
 //     maximum SQUARED speed (app/simulation_configuration.h:152-158,
 //     core/container/MeasuringFunctions.h:5-61);
 //   * cells_<i>.txt ("cell:c[start,end)", -1 for an empty cell) when
-//     bool_measure_neighborhood is set (app/simulation_configuration.h:34-45);
+//     bool_measure_neighborhood is set (app/simulation_configuration.h:34-45),
+//     and then also one line of neighbour and cell statistics of the last
+//     iteration in neighborhood_and_cells.data (AvgNeighborsPerParticle,
+//     core/algorithmic/MeasureAverageNeighborsPerParticle.h);
 //   * the timer summary on stdout and one appended line in timer_manager.data
 //     (core/utils/TimerManager.cpp:3-40).
 //
@@ -364,6 +367,9 @@ int main(int argc, char** argv) {
   const int gny = order == "morton" ? next_pow2(gny0) : gny0;
   const long long ncells = (long long)gnx * gny;
   std::vector<int32_t> keys;
+  struct {
+    long long num_cells = 0, num_empty = 0, avg_ppc = 0, min_ppc = 10000000, max_ppc = 0;
+  } cell_stats;
   auto write_cells = [&](long long step) {
     keys.resize(N);
     sphg_status s2 = sphg_get_debug(sim, SPHG_DBG_KEYS, keys.data(), nullptr);
@@ -377,6 +383,21 @@ int main(int argc, char** argv) {
     }
     std::ofstream f(outdir + "/cells_" + std::to_string(step) + ".txt");
     for (long long c = 0; c < ncells; ++c) f << "cell:" << c << "[" << cs[c] << "," << ce[c] << ")\n";
+    // cell statistics of AvgNeighborsPerParticle::MeasureCells
+    // (core/algorithmic/MeasureAverageNeighborsPerParticle.h:94-116)
+    long long sum = 0;
+    cell_stats.num_empty = 0;
+    cell_stats.min_ppc = 10000000;
+    cell_stats.max_ppc = 0;
+    for (long long c = 0; c < ncells; ++c) {
+      const long long k = ce[c] - cs[c];
+      sum += k;
+      cell_stats.max_ppc = std::max(cell_stats.max_ppc, k);
+      if (k > 0) cell_stats.min_ppc = std::min(cell_stats.min_ppc, k);
+      if (k == 0) ++cell_stats.num_empty;
+    }
+    cell_stats.num_cells = ncells;
+    cell_stats.avg_ppc = ncells ? sum / ncells : 0;
   };
   std::vector<int64_t> offs;
   std::vector<int32_t> idx;
@@ -485,6 +506,38 @@ int main(int argc, char** argv) {
   sphg_destroy(sim);
   timers.print();
   timers.append_file(outdir + "/timer_manager.data", steps, N);
+  if (measure && !offs.empty()) {
+    // AvgNeighborsPerParticle::Measure + PrintToFile on the last iteration's lists
+    // (core/algorithmic/MeasureAverageNeighborsPerParticle.h:66-92,118-134): neighbours
+    // per particle (self included), integer average, population standard deviation
+    long long sum = 0, mn = N, mx = 0;
+    for (long long i = 0; i < N; ++i) {
+      const long long k = offs[i + 1] - offs[i];
+      sum += k;
+      mn = std::min(mn, k);
+      mx = std::max(mx, k);
+    }
+    const long long avg = N ? sum / N : 0;
+    double dev = 0.0;
+    for (long long i = 0; i < N; ++i) {
+      const double k = (double)(offs[i + 1] - offs[i]) - (double)avg;
+      dev += k * k;
+    }
+    dev = N ? std::sqrt(dev / (double)N) : 0.0;
+    const std::string name = outdir + "/neighborhood_and_cells.data";
+    const bool fresh = !std::ifstream(name).good();
+    std::ofstream f(name, std::ios::app);
+    if (fresh) {
+      for (const char* c : {"avg_npp", "min_npp", "max_npp", "stddev_npp", "#cells", "#empty_cells", "avg_ppc",
+                            "min_ppc"})
+        f << std::fixed << std::setw(20) << std::left << c << "\t";
+      f << std::fixed << std::setw(20) << std::left << "max_ppc" << "\n";
+    }
+    f << std::fixed << std::setw(20) << std::left << avg << "\t" << std::setw(20) << mn << "\t" << std::setw(20) << mx
+      << "\t" << std::setw(20) << dev << "\t" << std::setw(20) << cell_stats.num_cells << "\t" << std::setw(20)
+      << cell_stats.num_empty << "\t" << std::setw(20) << cell_stats.avg_ppc << "\t" << std::setw(20)
+      << cell_stats.min_ppc << "\t" << std::setw(20) << cell_stats.max_ppc << "\n";
+  }
   if (writer.failed()) {
     std::cerr << "[Error] a checkpoint file could not be written" << std::endl;
     return 1;

@@ -91,6 +91,16 @@ def test_driver_matches_oracle_run(tmp_path, order, ctype):
                 assert start[int(c)] == w[0] and end[int(c)] == w[-1] + 1
             assert sum(1 for c in start if start[c] >= 0) == len(np.unique(k))
     assert os.path.exists(tmp_path / "timer_manager.data")
+    # neighbour and cell statistics of the last iteration (AvgNeighborsPerParticle columns)
+    lines = open(tmp_path / "neighborhood_and_cells.data").read().splitlines()
+    assert len(lines) == 2 and lines[0].split()[0] == "avg_npp"
+    vals = [float(v) for v in lines[1].split()]
+    r = sim.get()
+    sk = O.cell_ids(p, r["x"], r["y"])
+    s_, e_ = O.cell_ranges(p, sk)
+    offs, _ = O.neighbor_lists(p, r["x"], r["y"], sk, s_, e_)
+    npp = np.diff(offs)
+    assert vals[0] == int(npp.sum() // len(npp)) and vals[1] == npp.min() and vals[2] == npp.max()
 
 
 def test_driver_resume_from_snapshot_is_exact(tmp_path):
