@@ -47,9 +47,9 @@ UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
 # DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
 # summed over one iteration's kernels); filled from the committed profile summaries
-# (profiles/traffic_dam_break_1m.md: 107.4 MB per iteration of 1,000,000 particles,
+# (profiles/traffic_dam_break_1m.md: 107.2 MB per iteration of 1,000,000 particles,
 # caches flushed before each captured launch)
-TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 107.4}
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 107.2}
 L2_FLUSH_BYTES = 256 << 20
 
 
