@@ -228,6 +228,10 @@ sphg_status sphg_server_destroy(sphg_server* s);
 sphg_status sphg_server_submit(sphg_server* s, const sphg_params* p, int64_t n, const double* x,
                                const double* y, const double* vx, const double* vy, int64_t steps,
                                int64_t* request_id);
+/* The same for a state generated on the device at admission (sphg_upload_lattice's
+ * lattice, nx * ny particles): no host arrays cross the boundary for it. */
+sphg_status sphg_server_submit_lattice(sphg_server* s, const sphg_params* p, const sphg_lattice* spec,
+                                       int64_t steps, int64_t* request_id);
 /* Admit, step, retire.  *live = simulations live after the tick, *finished = retired by it. */
 sphg_status sphg_server_tick(sphg_server* s, void* stream, int32_t* live, int32_t* finished);
 /* Final state of a finished request (slot order, like sphg_download) and its

@@ -157,6 +157,8 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& f);
 char* host_stage(sphg_sim* s, size_t bytes);
 // In-cell offset o (FP64, in [0, cs)) as FP32, kept below cs after rounding.
 float split_offset(double o, double cs);
+// A lattice specification is valid for `count` particles (index: for the message).
+sphg_status check_lattice(const sphg_lattice& L, int64_t count, int index);
 // Instance holding particle i (instances are contiguous in particle order).
 int instance_of(const sphg_sim* s, int64_t i);
 uint32_t morton_host(uint32_t x, uint32_t y);

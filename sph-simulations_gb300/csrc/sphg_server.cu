@@ -61,7 +61,9 @@ struct SrvReq {
   int64_t id = 0;
   sphg_params p{};
   int64_t n = 0, steps = 0, runs = 0;
-  std::vector<double> x, y, vx, vy;           // initial state until admitted
+  std::vector<double> x, y, vx, vy;           // initial state until admitted (host arrays) ...
+  bool lattice = false;                        // ... or generated on the device at admission
+  sphg_lattice spec{};
   std::vector<double> rx, ry, rvx, rvy, rrho;  // result once done
   std::vector<int32_t> rids;
   double t_submit = 0, t_done = 0;
@@ -194,7 +196,7 @@ sphg_status repack(sphg_server* s, const std::vector<int64_t>& newlive, size_t n
     if (k < newlive.size() - nadmit) {
       src[k] = r.begin;
     } else {
-      stage_newcomer(s, r, L.desc[k], at);
+      if (!r.lattice) stage_newcomer(s, r, L.desc[k], at);
       src[k] = n_old + (int64_t)at;
       at += r.n;
     }
@@ -205,6 +207,16 @@ sphg_status repack(sphg_server* s, const std::vector<int64_t>& newlive, size_t n
     SPHG_CUDA(cudaMemcpyAsync(sim->keyTmp + n_old, s->hkey, nnew * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     if (sim->opt.track_ids)
       SPHG_CUDA(cudaMemcpyAsync(sim->idsA + n_old, s->hids, nnew * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    // lattice requests: generated in place on the device (after the copies above)
+    size_t off = 0;
+    for (size_t k = newlive.size() - nadmit; k < newlive.size(); ++k) {
+      const SrvReq& r = s->reqs[newlive[k]];
+      if (r.lattice)
+        SPHG_CUDA(sphg::launch_lattice_stage(L.desc[k], r.spec, sim->opt.precision, r.n, sim->posA + n_old + off,
+                                             sim->acc + n_old + off, sim->keyTmp + n_old + off,
+                                             sim->opt.track_ids ? sim->idsA + n_old + off : nullptr, st));
+      off += r.n;
+    }
   }
   // 3. new layout + gather table, then the gather
   SPHG_TRY(apply_layout(sim, (int)newlive.size(), p.data(), counts.data(), L, &st));
@@ -362,6 +374,30 @@ sphg_status sphg_server_submit(sphg_server* s, const sphg_params* p, int64_t n, 
   r.y.assign(y, y + n);
   r.vx.assign(vx, vx + n);
   r.vy.assign(vy, vy + n);
+  r.t_submit = now_s(s->t0);
+  s->reqs[r.id] = std::move(r);
+  s->queue.push_back(*id = s->next_id - 1);
+  return SPHG_OK;
+}
+
+sphg_status sphg_server_submit_lattice(sphg_server* s, const sphg_params* p, const sphg_lattice* spec,
+                                       int64_t steps, int64_t* id) {
+  if (!s || !p || !spec || steps < 1 || !id) return fail(SPHG_INVALID_ARG, "bad request (need steps >= 1)");
+  const int64_t n = spec->nx * spec->ny;
+  if (n <= 0) return fail(SPHG_INVALID_ARG, "empty lattice");
+  SPHG_TRY(check_lattice(*spec, n, 0));
+  InstDesc d;
+  uint64_t span = 0;
+  SPHG_TRY(make_desc(*p, 0, n, 0, d, span));
+  if ((size_t)n > s->sim->cap_n || span > s->sim->cap_keys)
+    return fail(SPHG_CAPACITY, "request larger than the whole server capacity");
+  SrvReq r;
+  r.id = s->next_id++;
+  r.p = *p;
+  r.n = n;
+  r.steps = steps;
+  r.lattice = true;
+  r.spec = *spec;
   r.t_submit = now_s(s->t0);
   s->reqs[r.id] = std::move(r);
   s->queue.push_back(*id = s->next_id - 1);

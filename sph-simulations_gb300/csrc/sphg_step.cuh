@@ -4,6 +4,7 @@
 #include <string>
 #include <cuda_runtime.h>
 
+#include "../../include/sphg.h"
 #include "sphg_common.cuh"
 
 namespace sphg {
@@ -87,6 +88,9 @@ cudaError_t launch_tiled(const StepArgs& a, int precision, bool force, cudaStrea
 size_t tile_smem_bytes(int tb, int cap, bool force);
 // Records the message returned by sphg_last_error_string() (sphg_api.cu).
 void set_last_error(const std::string& msg);
+// A served request's lattice initial state into the admission staging (sphg_init.cu).
+cudaError_t launch_lattice_stage(const InstDesc& d, const sphg_lattice& L, int precision, int64_t n, float2* pos,
+                                 float2* vel, uint32_t* key, int32_t* ids, cudaStream_t st);
 cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const float* y, int64_t n,
                                    int32_t* keys, cudaStream_t s);
 

@@ -115,6 +115,8 @@ def lib():
         L.sphg_delta_decode.argtypes = [_vp, _vp, ctypes.c_int64, _vp, _vp]
         L.sphg_autotune.argtypes = [ctypes.c_int32, PP, _lp, _dp, _dp, _dp, _dp, OP, ctypes.c_int32, OP,
                                     _dp, _vp]
+        L.sphg_server_submit_lattice.argtypes = [SP, PP, ctypes.POINTER(Lattice), ctypes.c_int64, _lp]
+        L.sphg_server_submit_lattice.restype = ctypes.c_int
         L.sphg_diagnostics_async.argtypes = [SP, _vp, _vp]
         L.sphg_diagnostics_async.restype = ctypes.c_int
         L.sphg_upload_lattice.argtypes = [SP, ctypes.POINTER(Lattice), _vp]
@@ -336,6 +338,14 @@ class Server:
         check(lib().sphg_server_submit(self._h, ctypes.byref(prm), len(x), _ptr(x), _ptr(y),
                                        _ptr(vx), _ptr(vy), int(steps), ctypes.byref(rid)))
         self.sizes[rid.value] = len(x)
+        return rid.value
+
+    def submit_lattice(self, prm, spec, steps):
+        """A request whose initial state the device generates at admission."""
+        rid = ctypes.c_int64(0)
+        check(lib().sphg_server_submit_lattice(self._h, ctypes.byref(prm), ctypes.byref(spec), int(steps),
+                                               ctypes.byref(rid)))
+        self.sizes[rid.value] = int(spec.nx * spec.ny)
         return rid.value
 
     def tick(self, stream=None):

@@ -109,3 +109,40 @@ def test_server_rejects_bad_requests():
         srv.submit(prm, big, big, big * 0, big * 0, 3)
     assert ei.value.status == S.CAPACITY
     srv.close()
+
+
+@pytest.mark.parametrize("prec", ["plain", "split"])
+def test_lattice_requests_equal_host_array_requests(prec):
+    """A request generated on the device at admission gives the same result as the
+    same lattice submitted as host arrays (and mixes with other requests)."""
+    import sphg as S
+    import workloads as W
+    from test_gpu_parity import _lattice_host
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    prm, x, y = W.dam_break_sized(1500, 1.2, 0.005, np.random.default_rng(3), alpha=0.1)
+    spec = S.lattice(0.0025, 0.0025, 0.005, 0.005, 30, 40, jitter=0.01, seed=77)
+    hx, hy = _lattice_host(spec.x0, spec.y0, spec.dx, spec.dy, spec.nx, spec.ny, spec.jitter, spec.seed)
+    out = []
+    for mode in ("lattice", "arrays"):
+        srv = S.Server(2e9, opts=S.options(precision=P))
+        other = srv.submit(S.params(**prm), x, y, np.zeros(len(x)), np.zeros(len(x)), 9)
+        if mode == "lattice":
+            rid = srv.submit_lattice(S.params(**prm), spec, 12)
+        else:
+            rid = srv.submit(S.params(**prm), hx, hy, np.zeros(len(hx)), np.zeros(len(hx)), 12)
+        res = None
+        for _ in range(100):
+            srv.tick()
+            res = srv.result(rid)
+            if res is not None:
+                break
+        assert res is not None
+        out.append(res)
+        srv.close()
+    a, b = out
+    assert (a["ids"] == b["ids"]).all()
+    for f in ("x", "y", "vx", "vy", "rho"):
+        if prec == "plain":
+            assert (a[f] == b[f]).all(), f
+        else:
+            np.testing.assert_allclose(a[f], b[f], rtol=1e-6, atol=1e-7 * np.abs(b[f]).max())
