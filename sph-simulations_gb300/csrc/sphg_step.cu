@@ -372,8 +372,31 @@ __device__ __forceinline__ void block_reduce6(double (&v)[6], double (*sh)[kDiag
   __syncthreads();
 }
 
+// Float-float arithmetic (Knuth's TwoSum, Dekker's Fast2Sum, products split
+// exactly with an FMA) for the per-thread part of the diagnostics.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+struct FFSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v, float err) {
+    float t, e;
+    two_sum(s, v, t, e);
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, err));
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // Per (chunk, instance) block.  The conservation sums (kinetic energy,
-// momentum) and max |v|^2 are FP64 from the FP32 velocities (products exact);
+// momentum) and max |v|^2 carry the FP32 velocities' exact squares in
+// float-float per thread and are reduced in FP64 across threads and blocks;
 // the in-domain count is decided in FP32 and redone in FP64 (out of line)
 // only within a thin band of a wall; counts are integers.
 static __device__ __noinline__ bool inside_d(double x, double y, const InstDesc& d) {
@@ -389,18 +412,30 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
   const int64_t per = (cnt + chunks - 1) / chunks;
   const int64_t b = d.begin + per * blockIdx.x;
   const int64_t e = min((int64_t)d.end, b + per);
-  double ek = 0.0, px = 0.0, py = 0.0, vmax = 0.0;
+  // Per-thread float-float accumulators (the products of the FP32 velocities are
+  // kept exactly as value + error): FP32 pipes for the elements, FP64 from the
+  // block reduction on.
+  FFSum s2, sx, sy;
+  float mh = 0.f, ml = 0.f;  // largest |v|^2 as a normalised float-float pair
   int inside = 0, bad = 0;
   const float band = 1.0e-6f * fmaxf(fabsf(d.hi_x - d.lo_x), fabsf(d.hi_y - d.lo_y));
   for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const float4 vel = a.velpA[i];
     const float2 p = a.posA[i];
-    const double vx = vel.x, vy = vel.y;
-    const double n2 = vx * vx + vy * vy;
-    ek += n2;
-    vmax = fmax(vmax, n2);
-    px += vx;
-    py += vy;
+    const float p1 = vel.x * vel.x, e1 = fmaf(vel.x, vel.x, -p1);
+    const float p2 = vel.y * vel.y, e2 = fmaf(vel.y, vel.y, -p2);
+    s2.add(p1, e1);
+    s2.add(p2, e2);
+    sx.add(vel.x, 0.f);
+    sy.add(vel.y, 0.f);
+    float h, l;
+    two_sum(p1, p2, h, l);
+    l += e1 + e2;
+    fast_two_sum(h, l, h, l);
+    if (h > mh || (h == mh && l > ml)) {
+      mh = h;
+      ml = l;
+    }
     int cx = 0, cy = 0;
     float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
     float lox = d.lo_x, hix = d.hi_x, loy = d.lo_y, hiy = d.hi_y;
@@ -423,7 +458,8 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
     inside += in ? 1 : 0;
     bad += fin ? 0 : 1;
   }
-  double v[6] = {0.5 * d.mass_d * ek, vmax, (double)inside, d.mass_d * px, d.mass_d * py, (double)bad};
+  double v[6] = {0.5 * d.mass_d * s2.value(), (double)mh + (double)ml, (double)inside, d.mass_d * sx.value(),
+                 d.mass_d * sy.value(), (double)bad};
   __shared__ double sh[6][kDiagThreads / 32];
   block_reduce6(v, sh);
   if (threadIdx.x < 6) partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = sh[threadIdx.x][0];
