@@ -116,6 +116,10 @@ void sphg_default_params(sphg_params* p);
 void sphg_default_options(sphg_options* o);
 const char* sphg_last_error_string(void);
 const char* sphg_version(void);
+/* out[6]: compute capability major, minor, SM count, and whether the device can
+ * read and write pageable host memory directly (cudaDevAttrPageableMemoryAccess,
+ * ...UsesHostPageTables, cudaDevAttrConcurrentManagedAccess). */
+sphg_status sphg_device_attributes(int32_t device, int32_t* out);
 
 /* One instance of n particles. */
 sphg_status sphg_create(const sphg_params* p, const sphg_options* o, int64_t n, sphg_sim** out);

@@ -645,6 +645,20 @@ const char* sphg_last_error_string(void) { return g_err.c_str(); }
 
 const char* sphg_version(void) { return "sphg 0.1 (sm_103a)"; }
 
+sphg_status sphg_device_attributes(int32_t device, int32_t* out) {
+  if (!out) return fail(SPHG_INVALID_ARG, "null argument");
+  const cudaDeviceAttr attrs[6] = {cudaDevAttrComputeCapabilityMajor, cudaDevAttrComputeCapabilityMinor,
+                                   cudaDevAttrMultiProcessorCount, cudaDevAttrPageableMemoryAccess,
+                                   cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                   cudaDevAttrConcurrentManagedAccess};
+  for (int k = 0; k < 6; ++k) {
+    int v = 0;
+    SPHG_CUDA(cudaDeviceGetAttribute(&v, attrs[k], device));
+    out[k] = v;
+  }
+  return SPHG_OK;
+}
+
 sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t* counts,
                               const sphg_options* o, sphg_sim** out) {
   if (!out || !p || !counts || ninst <= 0) return fail(SPHG_INVALID_ARG, "null argument or ninst <= 0");

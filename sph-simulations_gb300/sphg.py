@@ -119,6 +119,8 @@ def lib():
         L.sphg_server_submit_lattice.restype = ctypes.c_int
         L.sphg_diagnostics_async.argtypes = [SP, _vp, _vp]
         L.sphg_diagnostics_async.restype = ctypes.c_int
+        L.sphg_device_attributes.argtypes = [ctypes.c_int32, _ip]
+        L.sphg_device_attributes.restype = ctypes.c_int
         L.sphg_upload_lattice.argtypes = [SP, ctypes.POINTER(Lattice), _vp]
         L.sphg_upload_lattice.restype = ctypes.c_int
         L.sphg_cfl_dt.argtypes = [SP, ctypes.c_double, ctypes.c_double, _dp, _vp]
@@ -409,6 +411,13 @@ def autotune(prms, counts, x, y, vx, vy, base=None, steps=10, stream=None):
                               ctypes.byref(base if base is not None else options()), int(steps),
                               ctypes.byref(best), ctypes.byref(ms), _stream(stream)))
     return best, ms.value
+
+
+def device_attributes(device=0):
+    out = np.zeros(6, np.int32)
+    check(lib().sphg_device_attributes(int(device), _ptr(out, _ip)))
+    keys = ("cc_major", "cc_minor", "sms", "pageable_access", "pageable_uses_host_tables", "concurrent_managed")
+    return dict(zip(keys, out.tolist()))
 
 
 def delta_encode(offs_ptr, idx_ptr, n, enc_ptr, stream=None):
