@@ -645,6 +645,18 @@ const char* sphg_last_error_string(void) { return g_err.c_str(); }
 
 const char* sphg_version(void) { return "sphg 0.1 (sm_103a)"; }
 
+sphg_status sphg_set_host_access(sphg_sim* s, int32_t direct) {
+  if (!s) return fail(SPHG_INVALID_ARG, "null handle");
+  if (direct) {
+    int dev = 0, pageable = 0;
+    SPHG_CUDA(cudaGetDevice(&dev));
+    SPHG_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+    if (!pageable) return fail(SPHG_INVALID_ARG, "this device cannot access pageable host memory");
+  }
+  s->host_direct = direct != 0;
+  return SPHG_OK;
+}
+
 sphg_status sphg_device_attributes(int32_t device, int32_t* out) {
   if (!out) return fail(SPHG_INVALID_ARG, "null argument");
   const cudaDeviceAttr attrs[6] = {cudaDevAttrComputeCapabilityMajor, cudaDevAttrComputeCapabilityMinor,
@@ -682,6 +694,12 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
     return st;
   }
   st = apply_layout(s, ninst, p, counts, L, nullptr);
+  if (st == SPHG_OK) {
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
+      s->host_direct = pageable != 0;
+  }
   // set-up that would otherwise land on the first upload / step: the pinned
   // staging of upload and download, and the captured graph of an iteration
   if (st == SPHG_OK && s->n > 0 &&
@@ -707,7 +725,16 @@ sphg_status sphg_upload(sphg_sim* s, const double* x, const double* y, const dou
   if (!s || (s->n > 0 && (!x || !y || !vx || !vy))) return fail(SPHG_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = s->n;
-  if (n > 0) {
+  if (n > 0 && s->host_direct) {
+    uint32_t first_bad = 0;
+    SPHG_CUDA(cudaMemsetAsync(s->flags + 6, 0xff, sizeof(uint32_t), st));
+    SPHG_CUDA(sphg::launch_upload_direct(s->args(), s->opt.precision, x, y, vx, vy, s->flags + 6, st));
+    SPHG_CUDA(cudaMemsetAsync(s->scratch, 0, sizeof(uint32_t) * 4 * 256, st));
+    SPHG_CUDA(cudaMemcpyAsync(&first_bad, s->flags + 6, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+    if (first_bad != 0xffffffffu)
+      return fail(SPHG_NONFINITE, "non-finite value in the uploaded state at particle " + std::to_string(first_bad));
+  } else if (n > 0) {
     // pinned staging: positions (or split offsets), velocities, split cell keys, creation indices
     char* stg = host_stage(s, (size_t)n * (sizeof(float2) * 2 + sizeof(uint32_t) + sizeof(int32_t)));
     if (!stg) return fail(SPHG_OOM, "pinned host staging");
@@ -794,6 +821,12 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
   const int64_t n = s->n;
   if (n == 0) return SPHG_OK;
   const bool forces = fx || fy;
+  if (s->host_direct) {
+    if (forces) SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
+    SPHG_CUDA(sphg::launch_download_direct(s->args(), s->opt.precision, x, y, vx, vy, rho, fx, fy, ids, st));
+    SPHG_CUDA(cudaStreamSynchronize(st));
+    return device_errors(s, st);
+  }
   char* stg = host_stage(s, (size_t)n * (sizeof(float2) * 2 + sizeof(float4) + sizeof(float) + sizeof(uint32_t)));
   if (!stg) return fail(SPHG_OOM, "pinned host staging");
   float4* velp = reinterpret_cast<float4*>(stg);

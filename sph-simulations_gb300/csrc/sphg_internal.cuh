@@ -78,6 +78,9 @@ struct sphg_sim {
   int force_batched = 0;        // always use the per-instance-descriptor kernels
   int tile_bits = 0, tile_cap = 0, tile_grid = 0;
   bool uploaded = false, preloop_done = false;
+  // upload/download read and write the caller's arrays from the device
+  // (pageable host memory access), else through the pinned staging below
+  bool host_direct = false;
   // pinned host staging of upload/download (grows on demand)
   char* hstage = nullptr;
   size_t hstage_bytes = 0;

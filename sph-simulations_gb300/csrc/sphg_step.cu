@@ -399,15 +399,15 @@ struct FFSum {
 // float-float per thread and are reduced in FP64 across threads and blocks;
 // the in-domain count is decided in FP32 and redone in FP64 (out of line)
 // only within a thin band of a wall; counts are integers.
-static __device__ __noinline__ bool inside_d(double x, double y, const InstDesc& d) {
-  return !(x < d.lo_xd || x > d.hi_xd) && !(y < d.lo_yd || y > d.hi_yd);
+static __device__ __noinline__ bool inside_d(double x, double y, double lox, double hix, double loy, double hiy) {
+  return !(x < lox || x > hix) && !(y < loy || y > hiy);
 }
 
 template <int PREC>
 __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, int chunks,
                                                                   double* partials) {
   const int inst = blockIdx.y;
-  const InstDesc d = (a.ninst == 1) ? a.d0 : a.desc[inst];
+  const InstDesc& d = (a.ninst == 1) ? a.d0 : a.desc[inst];
   const int64_t cnt = d.end - d.begin;
   const int64_t per = (cnt + chunks - 1) / chunks;
   const int64_t b = d.begin + per * blockIdx.x;
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
     if (near) {
       const double xd = PREC == 1 ? d.lo_xd + cx * d.cs_xd + (double)x : (double)x;
       const double yd = PREC == 1 ? d.lo_yd + cy * d.cs_yd + (double)y : (double)y;
-      in = inside_d(xd, yd, d);
+      in = inside_d(xd, yd, d.lo_xd, d.hi_xd, d.lo_yd, d.hi_yd);
     }
     inside += in ? 1 : 0;
     bad += fin ? 0 : 1;

@@ -88,6 +88,11 @@ cudaError_t launch_tiled(const StepArgs& a, int precision, bool force, cudaStrea
 size_t tile_smem_bytes(int tb, int cap, bool force);
 // Records the message returned by sphg_last_error_string() (sphg_api.cu).
 void set_last_error(const std::string& msg);
+// Upload / download through the caller's host arrays from the device (sphg_hostio.cu).
+cudaError_t launch_upload_direct(const StepArgs& a, int precision, const double* x, const double* y,
+                                 const double* vx, const double* vy, uint32_t* first_bad, cudaStream_t st);
+cudaError_t launch_download_direct(const StepArgs& a, int precision, double* x, double* y, double* vx, double* vy,
+                                   double* rho, double* fx, double* fy, int32_t* ids, cudaStream_t st);
 // A served request's lattice initial state into the admission staging (sphg_init.cu).
 cudaError_t launch_lattice_stage(const InstDesc& d, const sphg_lattice& L, int precision, int64_t n, float2* pos,
                                  float2* vel, uint32_t* key, int32_t* ids, cudaStream_t st);

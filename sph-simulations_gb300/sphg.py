@@ -119,6 +119,8 @@ def lib():
         L.sphg_server_submit_lattice.restype = ctypes.c_int
         L.sphg_diagnostics_async.argtypes = [SP, _vp, _vp]
         L.sphg_diagnostics_async.restype = ctypes.c_int
+        L.sphg_set_host_access.argtypes = [SP, ctypes.c_int32]
+        L.sphg_set_host_access.restype = ctypes.c_int
         L.sphg_device_attributes.argtypes = [ctypes.c_int32, _ip]
         L.sphg_device_attributes.restype = ctypes.c_int
         L.sphg_upload_lattice.argtypes = [SP, ctypes.POINTER(Lattice), _vp]
@@ -278,6 +280,9 @@ class Sim:
         check(lib().sphg_neighbor_lists_encoded(self._h, _ptr(offs, _lp), _ptr(enc, _ip),
                                                 ctypes.byref(total), _stream(stream)))
         return offs, enc[:total.value]
+
+    def set_host_access(self, direct):
+        check(lib().sphg_set_host_access(self._h, int(direct)))
 
     def diagnostics_async(self, out_ptr, stream=None):
         """Enqueues the step header into pinned host memory at out_ptr (6 doubles per instance)."""

@@ -893,3 +893,34 @@ def test_particles_outside_the_high_walls(prec):
     assert np.max(np.abs(nx_ - ox)) < 1e-7 and np.max(np.abs(ny_ - oy)) < 1e-7
     assert (nx_ <= 0.3 + 1e-7).all() and (ny_ <= 0.3 + 1e-7).all()  # on the walls, within FP32 rounding
     sim.close()
+
+
+@pytest.mark.parametrize("prec", ["plain", "split"])
+def test_direct_host_access_equals_staging(prec):
+    """Upload/download converting the caller's arrays on the device (pageable host
+    memory access) give the staging path's results."""
+    S = _sphg()
+    if not S.device_attributes(0)["pageable_access"]:
+        pytest.skip("the device cannot access pageable host memory")
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    inst = _instances(seed=41)
+    prms = [S.params(**i[0]) for i in inst]
+    counts = [len(i[1]) for i in inst]
+    cat = [np.concatenate([i[k] for i in inst]) for k in (1, 2, 3, 4)]
+    outs = []
+    for direct in (1, 0):
+        sim = S.Sim(prms, counts, S.options(precision=P))
+        sim.set_host_access(direct)
+        sim.upload(*cat)
+        sim.preloop()
+        sim.step(7)
+        outs.append(sim.download())
+        bad = [c.copy() for c in cat]
+        bad[1][17] = np.nan
+        with pytest.raises(S.SphgError) as ei:
+            sim.upload(*bad)
+        assert ei.value.status == S.NONFINITE and "particle 17" in str(ei.value)
+        sim.close()
+    a, b = outs
+    for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
+        np.testing.assert_allclose(a[f], b[f], rtol=0, atol=1e-15 * max(1.0, np.abs(b[f]).max()))
