@@ -120,11 +120,14 @@ const char* sphg_version(void);
  * read and write pageable host memory directly (cudaDevAttrPageableMemoryAccess,
  * ...UsesHostPageTables, cudaDevAttrConcurrentManagedAccess). */
 sphg_status sphg_device_attributes(int32_t device, int32_t* out);
-/* Upload and download convert the caller's FP64 arrays on the device, reading
- * and writing them in place, when the device can access pageable host memory
- * (the default there; 1), or through a pinned staging buffer converted on
- * the host (0).  The results are the same. */
-sphg_status sphg_set_host_access(sphg_sim* s, int32_t direct);
+/* How upload and download reach the caller's FP64 arrays:
+ *   0: through a pinned staging buffer, converted on the host;
+ *   1: upload converts the caller's arrays on the device, reading them in place
+ *      (the default when the device can access pageable host memory);
+ *   2: download writes them from the device as well (fast when their pages are
+ *      already resident: writes into untouched pages fault them in one by one).
+ * The results are the same. */
+sphg_status sphg_set_host_access(sphg_sim* s, int32_t mode);
 
 /* One instance of n particles. */
 sphg_status sphg_create(const sphg_params* p, const sphg_options* o, int64_t n, sphg_sim** out);

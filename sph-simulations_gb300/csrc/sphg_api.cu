@@ -653,7 +653,7 @@ sphg_status sphg_set_host_access(sphg_sim* s, int32_t direct) {
     SPHG_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
     if (!pageable) return fail(SPHG_INVALID_ARG, "this device cannot access pageable host memory");
   }
-  s->host_direct = direct != 0;
+  s->host_direct = direct < 0 ? 0 : (direct > 2 ? 2 : direct);
   return SPHG_OK;
 }
 
@@ -698,7 +698,7 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
     int dev = 0, pageable = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
-      s->host_direct = pageable != 0;
+      s->host_direct = pageable != 0 ? 1 : 0;
   }
   // set-up that would otherwise land on the first upload / step: the pinned
   // staging of upload and download, and the captured graph of an iteration
@@ -821,7 +821,9 @@ sphg_status sphg_download(sphg_sim* s, double* x, double* y, double* vx, double*
   const int64_t n = s->n;
   if (n == 0) return SPHG_OK;
   const bool forces = fx || fy;
-  if (s->host_direct) {
+  if (s->host_direct == 2) {
+    // writes from the device into pages the host has not touched yet fault them
+    // in one by one, so the default download goes through the pinned staging
     if (forces) SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
     SPHG_CUDA(sphg::launch_download_direct(s->args(), s->opt.precision, x, y, vx, vy, rho, fx, fy, ids, st));
     SPHG_CUDA(cudaStreamSynchronize(st));

@@ -78,9 +78,10 @@ struct sphg_sim {
   int force_batched = 0;        // always use the per-instance-descriptor kernels
   int tile_bits = 0, tile_cap = 0, tile_grid = 0;
   bool uploaded = false, preloop_done = false;
-  // upload/download read and write the caller's arrays from the device
-  // (pageable host memory access), else through the pinned staging below
-  bool host_direct = false;
+  // 1: upload reads the caller's arrays from the device (pageable host memory
+  // access); 2: download writes them from the device too; 0: both through the
+  // pinned staging below
+  int host_direct = 0;
   // pinned host staging of upload/download (grows on demand)
   char* hstage = nullptr;
   size_t hstage_bytes = 0;
