@@ -313,9 +313,18 @@ def run_gpu(args):
     # ---- end to end through the C ABI from host buffers: upload of the initial
     #      state, pre-loop, every step followed by its step header (E_k, max|v|^2,
     #      N inside, momentum) copied into pinned host memory, final download
+    #      The result arrays are the caller's, allocated and touched once before
+    #      the timed region (like the pinned header buffer); where the GPU reads
+    #      and writes pageable host memory the download writes them directly.
     sim = sphg.Sim(sprm, w["counts"] if batched else n, opts)
     ninst = len(prm) if batched else 1
     headers = torch.empty((args.steps, 6 * ninst), dtype=torch.float64, pin_memory=True)
+    result = {k: np.empty(n, np.float64) for k in ("x", "y", "vx", "vy", "rho")}
+    result["ids"] = np.empty(n, np.int32)
+    for arr in result.values():
+        arr.fill(0)  # fault the pages in (np.zeros maps them lazily)
+    host_mode = 2 if sphg.device_attributes()["pageable_access"] else 0
+    sim.set_host_access(host_mode)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.upload(x, y, vx, vy, stream=sptr)
@@ -323,7 +332,7 @@ def run_gpu(args):
     for k in range(args.steps):
         sim.step(1, stream=sptr)
         sim.diagnostics_async(headers[k].data_ptr(), stream=sptr)
-    out = sim.download(forces=False, stream=sptr)  # synchronises; checks the device error words
+    out = sim.download(forces=False, stream=sptr, out=result)  # synchronises; checks the device error words
     e2e_s = time.perf_counter() - t0
     sim.close()
     hdr = headers.numpy()
@@ -333,7 +342,8 @@ def run_gpu(args):
     e2e = {"value": n * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(n * state_h2d / args.steps),
            "d2h_bytes_per_step": int(6 * 8 * ninst + n * state_d2h / args.steps),
-           "wall_s": e2e_s}
+           "wall_s": e2e_s,
+           "host_access": {0: "pinned staging", 2: "device reads and writes the caller's arrays"}[host_mode]}
     assert np.isfinite(out["x"]).all()
 
     hbm, src = peaks()

@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
       S.add(t * t * t);
     }
   } else {
+    __shared__ uint4 s_cells[9][kThreads];  // per thread: its non-empty stencil cells
     uint32_t* __restrict__ nbr = a.nbr;
     const uint32_t slots = (uint32_t)a.nbr_slots;
     const size_t n = (size_t)a.n;
@@ -157,9 +158,98 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
         ++cnt;
       }
     };
-    for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
-      accept((j << 5) | tag, r2);
-    });
+    if (n < ((size_t)1 << 27)) {
+      // One loop over the candidates of the non-empty stencil cells, cells in
+      // the stencil order and j ascending within a cell -- the visiting order of
+      // the cell-by-cell walk, so the sums are the same bits.  A warp then runs
+      // about max over its lanes of the candidate total instead of the sum over
+      // the nine cells of the per-cell maxima (cells hold 1-4 particles, so the
+      // per-cell loops kept half the lanes idle).  The cells are queued in
+      // shared memory as {j0 << 5 | tag, j1 << 5 | tag, shift x, shift y}; the
+      // pair is accumulated branch-free (the accepted share of candidates is
+      // about a third, so a branch would be taken by some lane nearly always).
+      const int tid = threadIdx.x;
+      const uint32_t code = key - d.cell_base;
+      decode_code(d, code, cx, cy);
+      const uint32_t ep = *a.epoch;
+      uint32_t c[9], valid, wrapmask;
+      stencil_keys(d, code, cx, cy, c, valid, wrapmask);
+      uint4 r[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) r[k] = ((valid >> k) & 1u) ? __ldg(a.ranges + c[k]) : make_uint4(0, 0, 0, 0);
+      int nseg = 0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        if (r[k].z == ep && r[k].y > r[k].x) {
+          const int c1 = k / 3 - 1, c2 = k % 3 - 1;
+          const uint32_t tag = (uint32_t)k | ((PREC == 0 && ((wrapmask >> k) & 1u)) ? 16u : 0u);
+          const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
+          const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
+          s_cells[nseg][tid] = make_uint4((r[k].x << 5) | tag, (r[k].y << 5) | tag, __float_as_uint(shx),
+                                          __float_as_uint(shy));
+          ++nseg;
+        }
+      }
+      const float2* __restrict__ pos = a.posA;
+      const float h2_lo = d.h2_lo, h2_hi = d.h2_hi;
+      const bool record = nbr != nullptr;
+      uint32_t jj = 0, je = 0;
+      float shx = 0.f, shy = 0.f;
+      int q = 0;
+      bool border = false;
+      while (true) {
+        if (jj == je) {
+          if (q == nseg) break;
+          const uint4 w = s_cells[q][tid];
+          ++q;
+          jj = w.x;
+          je = w.y;
+          shx = __uint_as_float(w.z);
+          shy = __uint_as_float(w.w);
+        }
+        const uint32_t j = jj >> 5;
+        const float2 pj = __ldg(pos + j);
+        float dx = (pi.x - pj.x) - shx;
+        float dy = (pi.y - pj.y) - shy;
+        float r2;
+        bool in;
+        if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
+          in = wrapped_pair(d, pi, pj, dx, dy);
+          r2 = fmaf(dx, dx, dy * dy);
+        } else {
+          r2 = fmaf(dx, dx, dy * dy);
+          in = r2 < h2_lo;
+          border |= !in && r2 <= h2_hi;
+        }
+        const float t = fmaf(-r2, inv_h2, 1.0f);
+        S.add(in ? t * t * t : 0.0f);
+        const bool rec = in && record && j != (uint32_t)i;
+        if (rec && cnt < slots) nbr[cnt * n + i] = jj;
+        cnt += rec ? 1u : 0u;
+        jj += 32u;
+      }
+      if (border) {  // rare: pairs in the FP64 band, the same cells in the same order
+#pragma unroll 1
+        for (int s = 0; s < nseg; ++s) {
+          const uint4 w = s_cells[s][tid];
+          const uint32_t tag = w.x & 31u;
+          if (PREC == 0 && (tag & 16u)) continue;
+          const int c1 = (int)(tag / 3) - 1, c2 = (int)(tag % 3) - 1;
+          const float sx = __uint_as_float(w.z), sy = __uint_as_float(w.w);
+          for (uint32_t e = w.x; e != w.y; e += 32u) {
+            const float2 pj = __ldg(pos + (e >> 5));
+            const float dx = (pi.x - pj.x) - sx;
+            const float dy = (pi.y - pj.y) - sy;
+            const float r2 = fmaf(dx, dx, dy * dy);
+            if (r2 >= h2_lo && r2 <= h2_hi && pair_inside<PREC>(d, pi, pj, c1, c2, r2)) accept(e, r2);
+          }
+        }
+      }
+    } else {
+      for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float, float, float r2, uint32_t tag) {
+        accept((j << 5) | tag, r2);
+      });
+    }
     if (nbr) a.ncount[i] = cnt;
   }
   float rho, drho;

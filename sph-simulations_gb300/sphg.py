@@ -228,13 +228,24 @@ class Sim:
     def step(self, k=1, stream=None):
         check(lib().sphg_step(self._h, int(k), _stream(stream)))
 
-    def download(self, forces=True, stream=None):
+    def download(self, forces=True, stream=None, out=None):
+        """Current state as FP64 arrays in slot order.  out: optional dict of the
+        caller's arrays to fill (x, y, vx, vy, rho, ids, and fx, fy with forces),
+        each C-contiguous with n entries of the right type; reused buffers whose
+        pages are resident let host-access mode 2 write them from the device."""
         n = self.n
-        out = {k: np.empty(n, np.float64) for k in ("x", "y", "vx", "vy", "rho")}
-        if forces:
-            out["fx"] = np.empty(n, np.float64)
-            out["fy"] = np.empty(n, np.float64)
-        ids = np.empty(n, np.int32)
+        names = ("x", "y", "vx", "vy", "rho") + (("fx", "fy") if forces else ())
+        if out is None:
+            out = {k: np.empty(n, np.float64) for k in names}
+            ids = np.empty(n, np.int32)
+        else:
+            for k in names:
+                a = out[k]
+                if a.dtype != np.float64 or a.shape != (n,) or not a.flags.c_contiguous:
+                    raise ValueError(f"download: out[{k!r}] must be a contiguous float64 array of {n}")
+            ids = out.get("ids")
+            if ids is None or ids.dtype != np.int32 or ids.shape != (n,) or not ids.flags.c_contiguous:
+                raise ValueError(f"download: out['ids'] must be a contiguous int32 array of {n}")
         check(lib().sphg_download(self._h, _ptr(out["x"]), _ptr(out["y"]), _ptr(out["vx"]),
                                   _ptr(out["vy"]), _ptr(out["rho"]),
                                   _ptr(out["fx"]) if forces else None,
@@ -281,8 +292,10 @@ class Sim:
                                                 ctypes.byref(total), _stream(stream)))
         return offs, enc[:total.value]
 
-    def set_host_access(self, direct):
-        check(lib().sphg_set_host_access(self._h, int(direct)))
+    def set_host_access(self, mode):
+        """0: pinned staging; 1: upload reads the caller's arrays from the device;
+        2: download writes them from the device as well."""
+        check(lib().sphg_set_host_access(self._h, int(mode)))
 
     def diagnostics_async(self, out_ptr, stream=None):
         """Enqueues the step header into pinned host memory at out_ptr (6 doubles per instance)."""
