@@ -236,6 +236,7 @@ sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond
   m.msorted = s->msorted;
   m.ctl = s->flags + 3;
   m.epoch = s->flags + 2;
+  m.ranges = s->ranges;
   m.keyS = s->keyTmp;
   m.perm = s->perm;
   m.cond = cond;

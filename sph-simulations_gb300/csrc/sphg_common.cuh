@@ -125,6 +125,15 @@ struct CSum {
     s = sn;
     c = __fadd_rn(c, err);
   }
+  // Fast2Sum (Dekker): the rounding error of s + t is exactly t - ((s + t) - s)
+  // when |s| >= |t|.  Valid for the density sum once it holds the particle's
+  // own term W(0) = 1: every other term (1 - r^2/h^2)^3 of an accepted pair
+  // lies in [0, 1] and none is negative.
+  __device__ __forceinline__ void add_fast(float t) {
+    const float sn = __fadd_rn(s, t);
+    c = __fadd_rn(c, __fsub_rn(t, __fsub_rn(sn, s)));
+    s = sn;
+  }
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
@@ -132,6 +141,7 @@ struct PSum {
   float s;
   __device__ __forceinline__ PSum() : s(0.f) {}
   __device__ __forceinline__ void add(float t) { s += t; }
+  __device__ __forceinline__ void add_fast(float t) { s += t; }
   __device__ __forceinline__ float value() const { return s; }
 };
 

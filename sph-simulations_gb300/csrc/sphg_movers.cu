@@ -43,31 +43,50 @@ __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p,
   return a.wprefix[w] + __popc(a.mask[w] & below);
 }
 
-// Slot `from` of the integrated state to sorted position `to`.
-__device__ __forceinline__ void place(const MoverArgs& a, int64_t from, int64_t to, uint32_t key) {
+// Slot `from` of the integrated state (its values p, v, id) to sorted position `to`.
+__device__ __forceinline__ void place_values(const MoverArgs& a, int64_t from, int64_t to, uint32_t key, float2 p,
+                                             float2 v, int32_t id) {
   a.keyS[to] = key;
   a.perm[to] = (uint32_t)from;
-  a.posA[to] = a.posB[from];
-  const float2 v = a.velB[from];
+  a.posA[to] = p;
   a.velpA[to] = make_float4(v.x, v.y, 0.f, 0.f);
-  if (a.idsA) a.idsA[to] = a.idsB[from];
+  if (a.idsA) a.idsA[to] = id;
 }
 
-// Movers ordered before v (a count in [lo, hi] of the sorted mover list), by a
-// warp-wide 32-way search: two or three dependent rounds for 8,192 movers.
-__device__ __forceinline__ uint32_t warp_count_below(const unsigned long long* __restrict__ ms, uint32_t lo,
-                                                     uint32_t hi, unsigned long long v, int lane) {
-  while (hi - lo > 32) {
-    const uint32_t step = (hi - lo + 31) / 32;
-    const uint32_t pos = lo + (uint32_t)(lane + 1) * step - 1;
-    const bool less = pos < hi && __ldg(ms + pos) < v;
-    const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, less));
-    const uint32_t nhi = lo + (cnt + 1) * step - 1;
-    lo += cnt * step;
-    if (nhi < hi) hi = nhi;
+__device__ __forceinline__ void place(const MoverArgs& a, int64_t from, int64_t to, uint32_t key) {
+  place_values(a, from, to, key, a.posB[from], a.velB[from], a.idsA ? a.idsB[from] : 0);
+}
+
+// Movers ordered before va and before vb: counts in [0, m] of the sorted mover
+// list, by warp-wide 32-way searches (two dependent rounds for 8,192 movers);
+// the two searches are interleaved so their load rounds overlap.
+__device__ __forceinline__ void warp_count_below2(const unsigned long long* __restrict__ ms, uint32_t m,
+                                                  unsigned long long va, unsigned long long vb, int lane,
+                                                  uint32_t& ra, uint32_t& rb) {
+  uint32_t la = 0, ha = m, lb = 0, hb = m;
+  while (ha - la > 32 || hb - lb > 32) {
+    const bool wa = ha - la > 32, wb = hb - lb > 32;
+    const uint32_t sa = (ha - la + 31) / 32, sb = (hb - lb + 31) / 32;
+    const uint32_t pa = la + (uint32_t)(lane + 1) * sa - 1, pb = lb + (uint32_t)(lane + 1) * sb - 1;
+    const bool lessa = wa && pa < ha && __ldg(ms + pa) < va;
+    const bool lessb = wb && pb < hb && __ldg(ms + pb) < vb;
+    const uint32_t ca = __popc(__ballot_sync(0xffffffffu, lessa));
+    const uint32_t cb = __popc(__ballot_sync(0xffffffffu, lessb));
+    if (wa) {
+      const uint32_t nh = la + (ca + 1) * sa - 1;
+      la += ca * sa;
+      if (nh < ha) ha = nh;
+    }
+    if (wb) {
+      const uint32_t nh = lb + (cb + 1) * sb - 1;
+      lb += cb * sb;
+      if (nh < hb) hb = nh;
+    }
   }
-  const bool less = lo + (uint32_t)lane < hi && __ldg(ms + lo + lane) < v;
-  return lo + __popc(__ballot_sync(0xffffffffu, less));
+  const bool lessa = la + (uint32_t)lane < ha && __ldg(ms + la + lane) < va;
+  const bool lessb = lb + (uint32_t)lane < hb && __ldg(ms + lb + lane) < vb;
+  ra = la + __popc(__ballot_sync(0xffffffffu, lessa));
+  rb = lb + __popc(__ballot_sync(0xffffffffu, lessb));
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* sh) {
@@ -160,7 +179,21 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
   for (uint32_t q = lane; q < m; q += 32) c += __ldg(a.movers + q) < v;
   const uint32_t rank = __reduce_add_sync(0xffffffffu, c);
   const uint32_t k = (uint32_t)(v >> 32), sl = (uint32_t)v;
-  // p = number of slots s with (keyA[s], s) < (k, sl)
+  // p = number of slots s with (keyA[s], s) < (k, sl).  When cell k holds
+  // particles in the current order, its range [start, end) gives p directly
+  // (movers_compact has bumped the epoch, so the current ranges carry the
+  // previous one); otherwise a warp-wide search of the keys finds it.
+  const uint4 cr = __ldg(a.ranges + k);
+  if (cr.z == *a.epoch - 1u && cr.x < cr.y && cr.y <= a.n) {
+    if (lane == 0) {
+      const int64_t p = sl < cr.x ? cr.x : (sl > cr.y ? cr.y : sl);
+      if (rank < m) a.msorted[rank] = v;
+      const int64_t fin = (int64_t)rank + (p - (int64_t)movers_before(a, p, m));
+      if (rank < m && fin >= 0 && fin < a.n && sl < a.n) place(a, sl, fin, k);
+      else a.ctl[2] = 1u;
+    }
+    return;
+  }
   int64_t lo = 0, hi = a.n;
   while (hi - lo > 32) {
     const int64_t step = (hi - lo + 31) / 32;
@@ -192,25 +225,39 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
 }
 
 // Thread i places slot i if it kept its key (the movers are placed already).
+// A stayer's position is its rank among stayers + the movers ordered before
+// it.  A warp's slots are consecutive, so the movers ordered before any of them
+// lie between the counts of its first and last slot: two interleaved warp-wide
+// searches per warp, then each lane refines inside that (usually empty)
+// interval.  Everything that does not depend on the searches is loaded first.
 __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   cudaGridDependencySynchronize();  // the sorted movers of movers_rank_place
   if (!a.ctl[0]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m = a.ctl[1];
-  // a stayer: its rank among stayers + the movers ordered before it.  A warp's
-  // slots are consecutive, so the movers ordered before any of them lie
-  // between the counts of its first and last slot: two warp-wide searches per
-  // warp, then each lane refines inside that (usually empty) interval.
   const int lane = threadIdx.x & 31;
   const int64_t w0 = i - lane;
   if (w0 >= a.n) return;  // the whole warp is past the last slot
-  const int64_t w1 = min(w0 + 31, a.n - 1);
-  const unsigned long long v0 = ((unsigned long long)a.keyA[w0] << 32) | (uint32_t)w0;
-  const unsigned long long v1 = ((unsigned long long)a.keyA[w1] << 32) | (uint32_t)w1;
-  const uint32_t wlo = warp_count_below(a.msorted, 0, m, v0, lane);
-  const uint32_t whi = warp_count_below(a.msorted, wlo, m, v1, lane);
-  if (i >= a.n || ((a.mask[i >> 5] >> (i & 31)) & 1u)) return;
-  const uint32_t k = a.keyA[i];
+  const bool valid = i < a.n;
+  const uint32_t k = valid ? a.keyA[i] : 0xFFFFFFFFu;
+  const uint32_t mw = valid ? a.mask[i >> 5] : 0xFFFFFFFFu;
+  const bool stay = valid && !((mw >> lane) & 1u);
+  uint32_t before = 0;
+  float2 p = make_float2(0.f, 0.f), vel = make_float2(0.f, 0.f);
+  int32_t id = 0;
+  if (stay) {
+    before = a.wprefix[i >> 5] + __popc(mw & ((1u << lane) - 1u));
+    p = a.posB[i];
+    vel = a.velB[i];
+    if (a.idsA) id = a.idsB[i];
+  }
+  const int last = (int)(min(w0 + 31, a.n - 1) - w0);
+  const unsigned long long v0 = ((unsigned long long)__shfl_sync(0xffffffffu, k, 0) << 32) | (uint32_t)w0;
+  const unsigned long long v1 =
+      ((unsigned long long)__shfl_sync(0xffffffffu, k, last) << 32) | (uint32_t)(w0 + last);
+  uint32_t wlo, whi;
+  warp_count_below2(a.msorted, m, v0, v1, lane, wlo, whi);
+  if (!stay) return;
   const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
   uint32_t lo = wlo, hi = whi;
   while (lo < hi) {
@@ -218,8 +265,8 @@ __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
     if (a.msorted[mid] < v) lo = mid + 1;
     else hi = mid;
   }
-  const int64_t fin = i - (int64_t)movers_before(a, i, m) + lo;
-  if (fin >= 0 && fin < a.n) place(a, i, fin, k);
+  const int64_t fin = i - (int64_t)before + lo;
+  if (fin >= 0 && fin < a.n) place_values(a, i, fin, k, p, vel, id);
   else a.ctl[2] = 1u;
 }
 

@@ -20,6 +20,7 @@ struct MoverArgs {
   uint32_t* ctl;           // [0] = 1 when the incremental path ran, [1] = changed slots,
                            // [2] set to 1 if a record was inconsistent (never cleared here)
   uint32_t* epoch;         // step epoch of the cell-range table
+  const uint4* ranges;     // cell ranges {start, end, epoch, 0} of the current sorted order
   uint32_t* keyS;          // out: sorted keys
   uint32_t* perm;          // out: previous slot of each sorted position
   unsigned long long cond; // graph conditional handle of the full sort (0: none), set to

@@ -160,14 +160,17 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
     };
     if (n < ((size_t)1 << 27)) {
       // One loop over the candidates of the non-empty stencil cells, cells in
-      // the stencil order and j ascending within a cell -- the visiting order of
-      // the cell-by-cell walk, so the sums are the same bits.  A warp then runs
-      // about max over its lanes of the candidate total instead of the sum over
-      // the nine cells of the per-cell maxima (cells hold 1-4 particles, so the
-      // per-cell loops kept half the lanes idle).  The cells are queued in
+      // the stencil order and j ascending within a cell.  A warp then runs about
+      // max over its lanes of the candidate total instead of the sum over the
+      // nine cells of the per-cell maxima (cells hold 1-4 particles, so
+      // per-cell loops keep half the lanes idle).  The cells are queued in
       // shared memory as {j0 << 5 | tag, j1 << 5 | tag, shift x, shift y}; the
-      // pair is accumulated branch-free (the accepted share of candidates is
-      // about a third, so a branch would be taken by some lane nearly always).
+      // position of the next candidate is loaded one iteration ahead; pairs are
+      // accumulated branch-free (about a third of the candidates are accepted,
+      // so a branch would be taken by some lane nearly always).  In split
+      // precision the particle's own term W(0) = 1 is the first term of the
+      // compensated sum (which then needs only Fast2Sum) and is skipped in the
+      // walk; plain sums add it where the walk meets it.
       const int tid = threadIdx.x;
       const uint32_t code = key - d.cell_base;
       decode_code(d, code, cx, cy);
@@ -193,40 +196,62 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
       const float2* __restrict__ pos = a.posA;
       const float h2_lo = d.h2_lo, h2_hi = d.h2_hi;
       const bool record = nbr != nullptr;
-      uint32_t jj = 0, je = 0;
-      float shx = 0.f, shy = 0.f;
-      int q = 0;
+      const uint32_t self = (uint32_t)i;
+      uint32_t* rp = record ? nbr + i : nullptr;  // next record slot: nbr[cnt * n + i]
       bool border = false;
-      while (true) {
-        if (jj == je) {
-          if (q == nseg) break;
-          const uint4 w = s_cells[q][tid];
-          ++q;
-          jj = w.x;
-          je = w.y;
-          shx = __uint_as_float(w.z);
-          shy = __uint_as_float(w.w);
+      if (PREC == 1) S.add(1.0f);  // own term W(0) first (plain sums keep the walk's order)
+      if (nseg > 0) {  // always: the particle's own cell holds it
+        uint4 w = s_cells[0][tid];
+        int q = 1;
+        uint32_t jj = w.x, je = w.y;
+        float shx = __uint_as_float(w.z), shy = __uint_as_float(w.w);
+        float2 pj = __ldg(pos + (jj >> 5));
+        while (true) {
+          uint32_t jn = jj + 32u, jen = je;
+          float shxn = shx, shyn = shy;
+          bool more = true;
+          if (jn == je) {
+            if (q == nseg) {
+              more = false;
+            } else {
+              w = s_cells[q][tid];
+              ++q;
+              jn = w.x;
+              jen = w.y;
+              shxn = __uint_as_float(w.z);
+              shyn = __uint_as_float(w.w);
+            }
+          }
+          const float2 pn = __ldg(pos + ((more ? jn : jj) >> 5));  // one candidate ahead
+          const uint32_t j = jj >> 5;
+          float dx = (pi.x - pj.x) - shx;
+          float dy = (pi.y - pj.y) - shy;
+          float r2;
+          bool in;
+          if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
+            in = wrapped_pair(d, pi, pj, dx, dy);
+            r2 = fmaf(dx, dx, dy * dy);
+          } else {
+            r2 = fmaf(dx, dx, dy * dy);
+            in = r2 < h2_lo;
+            border |= !in && r2 <= h2_hi;
+          }
+          const bool other = j != self;
+          const float t = fmaf(-r2, inv_h2, 1.0f);
+          S.add_fast((PREC == 1 ? in && other : in) ? t * t * t : 0.0f);
+          const bool rec = in && other && record;
+          if (rec && cnt < slots) {
+            *rp = jj;
+            rp += n;
+          }
+          cnt += rec ? 1u : 0u;
+          if (!more) break;
+          jj = jn;
+          je = jen;
+          shx = shxn;
+          shy = shyn;
+          pj = pn;
         }
-        const uint32_t j = jj >> 5;
-        const float2 pj = __ldg(pos + j);
-        float dx = (pi.x - pj.x) - shx;
-        float dy = (pi.y - pj.y) - shy;
-        float r2;
-        bool in;
-        if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
-          in = wrapped_pair(d, pi, pj, dx, dy);
-          r2 = fmaf(dx, dx, dy * dy);
-        } else {
-          r2 = fmaf(dx, dx, dy * dy);
-          in = r2 < h2_lo;
-          border |= !in && r2 <= h2_hi;
-        }
-        const float t = fmaf(-r2, inv_h2, 1.0f);
-        S.add(in ? t * t * t : 0.0f);
-        const bool rec = in && record && j != (uint32_t)i;
-        if (rec && cnt < slots) nbr[cnt * n + i] = jj;
-        cnt += rec ? 1u : 0u;
-        jj += 32u;
       }
       if (border) {  // rare: pairs in the FP64 band, the same cells in the same order
 #pragma unroll 1
