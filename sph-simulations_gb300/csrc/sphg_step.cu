@@ -292,36 +292,30 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- forces (+ integration)
-// Accepted neighbours of a thread are first collected in shared memory
-// (dx, dy, j) by the cheap candidate scan, then the pair forces run over that
-// list: the warp executes the heavy per-pair math about max-over-lanes(count)
-// times instead of once per candidate iteration.  A thread with more than
-// kForceBuf neighbours handles the extra ones inline during the scan.
+// The pairs are the neighbours the density pass recorded (j << 5 | stencil
+// tag per entry); a particle with more than the recorded slots walks the
+// stencil again.
 static_assert(((1 << kGroupShift) % kThreads) == 0, "a force block lies inside one mover group");
-constexpr int kForceBuf = 12;
 #ifndef SPHG_FORCE_BATCH
 #define SPHG_FORCE_BATCH 4
 #endif
 constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered together
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
-                                              uint32_t (*bj)[kThreads]);
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i);
 
 // Four blocks per SM (64 registers) for one instance, three for the batched
 // variants (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs a) {
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
-  __shared__ float2 bd[kForceBuf][kThreads];
-  __shared__ uint32_t bj[kForceBuf][kThreads];
   __shared__ uint32_t moved_in_block;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
   if (track && threadIdx.x == 0) moved_in_block = 0;
   uint32_t key = 0;
-  if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, bd, bj);
+  if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i);
   if (track) {
     // slots whose cell key changed, for the incremental re-sort: one bit per
     // slot (a warp holds 32 consecutive slots), one count per block
@@ -339,8 +333,7 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs
 // Forces on particle i; in integrate mode also the update and the new key
 // (returned), in force-only mode the acceleration is stored.
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, float2 (*bd)[kThreads],
-                                              uint32_t (*bj)[kThreads]) {
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
   // one instance: a copy of the kernel-argument descriptor; batched: a reference
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
   const uint32_t key = a.keyA[i];
@@ -400,14 +393,18 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
     // the density pass recorded this particle's neighbours (stencil order)
     decode_code(d, key - d.cell_base, cx, cy);
     const size_t n = (size_t)a.n;
-    uint32_t q = 0;
-    // kForceBatch neighbours at a time: their gathers are in flight together
-    for (; q + kForceBatch <= cnt; q += kForceBatch) {
+    // kForceBatch neighbours at a time, their gathers in flight together.  The
+    // lanes of a warp all run the warp's largest count rounded up to whole
+    // batches; a lane's missing entries are the particle itself (stencil cell
+    // 4, no shift), whose pair term is exactly zero (r = 0, v_j = v_i).
+    const uint32_t wmax = __reduce_max_sync(__activemask(), cnt);
+    const uint32_t self_e = ((uint32_t)i << 5) | 4u;
+    for (uint32_t q = 0; q < wmax; q += kForceBatch) {
       uint32_t e[kForceBatch];
       float2 pj[kForceBatch];
       float4 vj[kForceBatch];
 #pragma unroll
-      for (int u = 0; u < kForceBatch; ++u) e[u] = __ldg(a.nbr + (q + u) * n + i);
+      for (int u = 0; u < kForceBatch; ++u) e[u] = q + u < cnt ? __ldg(a.nbr + (q + u) * n + i) : self_e;
 #pragma unroll
       for (int u = 0; u < kForceBatch; ++u) {
         pj[u] = __ldg(a.posA + (e[u] >> 5));
@@ -420,29 +417,12 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, floa
         pair_v(vj[u], dx, dy);
       }
     }
-    for (; q < cnt; ++q) {
-      const uint32_t e = __ldg(a.nbr + q * n + i);
-      float dx, dy;
-      entry_vec<PREC>(d, pi, __ldg(a.posA + (e >> 5)), e, dx, dy);
-      pair(e >> 5, dx, dy);
-    }
   } else {
-    int nb = 0;
-    const int t = threadIdx.x;
+    // more neighbours than the density pass could record (or no record): the
+    // stencil walk, pairs in the walk's order
     for_each_neighbor<PREC>(a, d, key, pi, cx, cy, [&](uint32_t j, float dx, float dy, float, uint32_t) {
-      if (j == (uint32_t)i) return;
-      if (nb < kForceBuf) {
-        bd[nb][t] = make_float2(dx, dy);
-        bj[nb][t] = j;
-        ++nb;
-      } else {
-        pair(j, dx, dy);
-      }
+      if (j != (uint32_t)i) pair(j, dx, dy);
     });
-    for (int q = 0; q < nb; ++q) {
-      const float2 dd = bd[q][t];
-      pair(bj[q][t], dd.x, dd.y);
-    }
   }
   const float ax = d.gx + fx.value();
   const float ay = d.gy + fy.value();
