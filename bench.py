@@ -46,10 +46,9 @@ METRIC = ("particle-steps/s on 1 GB300, batched vs plain GPU path at ≤1e-5 rel
 UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
 # DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
-# summed over one iteration's kernels); filled from the committed profile summaries
-# (profiles/traffic_dam_break_1m.md: 107.2 MB per iteration of 1,000,000 particles,
-# caches flushed before each captured launch)
-TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 107.2}
+# summed over one merge-path iteration's kernels, caches flushed before each captured
+# launch): 106.0 MB per iteration of 1,000,000 particles
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 106.0}
 L2_FLUSH_BYTES = 256 << 20
 
 
