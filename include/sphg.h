@@ -174,6 +174,18 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream);
  * valid until the stream passes this point) in stream order, so a step loop
  * reads every step's header without a host synchronisation per step. */
 sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream);
+/* nsteps main-loop iterations, each followed by its step header (the 6 values
+ * of sphg_diagnostics per instance) written to out[(k * ninst + inst) * 6 ..]
+ * for iteration k -- the reference's main loop, which prints a header after
+ * every iteration (app/simulation_configuration.h:431-433).  out holds
+ * nsteps * 6 * ninst doubles; the values land in stream order.  Where the
+ * device can write out (pinned host memory, or pageable memory on a node with
+ * pageable access) the kernels write it directly and the iterations replay as
+ * one graph each; otherwise each header is copied. */
+sphg_status sphg_step_headers(sphg_sim* s, int64_t nsteps, double* out, void* stream);
+/* Waits for the work enqueued on stream (for hosts without a CUDA runtime of
+ * their own, such as ctypes callers of the asynchronous entry points). */
+sphg_status sphg_stream_synchronize(void* stream);
 
 /* Adaptive time step per instance from the current state: FP64 maxima of the
  * speed and of the acceleration on the device, then

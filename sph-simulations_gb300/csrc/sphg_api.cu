@@ -321,10 +321,20 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
   return enqueue_after_sort(s, st, ev);
 }
 
+// The step header of the current state into the header slot (graph-capturable).
+sphg_status enqueue_header(sphg_sim* s, cudaStream_t st) {
+  int64_t max_n = 0;
+  for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
+  SPHG_CUDA(sphg::launch_diagnostics_slot(s->args(), s->opt.precision, s->diag_partials,
+                                          sphg::diag_chunks(max_n, s->diag_chunks), s->hslot, st));
+  return SPHG_OK;
+}
+
 // Graph of one iteration with the full sort under a conditional node: the
 // incremental re-sort's decision kernel switches it off, so iterations that
 // merge launch none of the full sort's kernels.
-sphg_status build_graph_conditional(sphg_sim* s) {
+
+sphg_status build_graph_conditional(sphg_sim* s, cudaGraphExec_t* exec, bool header) {
   if (!s->cap_stream2) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream2, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
   SPHG_CUDA(cudaGraphCreate(&g, 0));
@@ -375,37 +385,42 @@ sphg_status build_graph_conditional(sphg_sim* s) {
   if (cudaStreamUpdateCaptureDependencies(s->cap_stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
     return done(fail(SPHG_CUDA_ERROR, "capture dependencies"));
   st = enqueue_after_sort(s, s->cap_stream, nullptr);
+  if (st == SPHG_OK && header) st = enqueue_header(s, s->cap_stream);
   if (st != SPHG_OK) return done(st);
   cudaGraph_t out = nullptr;
   if (cudaStreamEndCapture(s->cap_stream, &out) != cudaSuccess) return done(fail(SPHG_CUDA_ERROR, "end capture"));
-  const cudaError_t e = cudaGraphInstantiate(&s->gexec, g, 0);
+  const cudaError_t e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   g = nullptr;
   if (e != cudaSuccess) {
-    s->gexec = nullptr;
+    *exec = nullptr;
     return fail(SPHG_CUDA_ERROR, std::string("instantiate: ") + cudaGetErrorString(e));
   }
   return SPHG_OK;
 }
 
-sphg_status build_graph(sphg_sim* s) {
-  if (s->gexec) return SPHG_OK;
+// The graph of one iteration (header: followed by its step header into the
+// header slot).
+sphg_status build_graph(sphg_sim* s, bool header = false) {
+  cudaGraphExec_t* exec = header ? &s->gexec_hdr : &s->gexec;
+  if (*exec) return SPHG_OK;
   if (!s->cap_stream) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
   if (s->movers_on && s->cond_graph) {
-    if (build_graph_conditional(s) == SPHG_OK) return SPHG_OK;
+    if (build_graph_conditional(s, exec, header) == SPHG_OK) return SPHG_OK;
     s->cond_graph = false;  // not available here: the full sort's kernels skip themselves instead
     cudaGetLastError();
   }
   cudaGraph_t g = nullptr;
   SPHG_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
   sphg_status st = enqueue_step(s, s->cap_stream);
+  if (st == SPHG_OK && header) st = enqueue_header(s, s->cap_stream);
   cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
   if (st != SPHG_OK) {
     if (g) cudaGraphDestroy(g);
     return st;
   }
   SPHG_CUDA(e);
-  e = cudaGraphInstantiate(&s->gexec, g, 0);
+  e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   SPHG_CUDA(e);
   return SPHG_OK;
@@ -505,6 +520,7 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     s->flags = A.take<uint32_t>(16);
     s->diag_partials = A.take<double>((size_t)ninst * s->diag_chunks * 6);
     s->diag_out = A.take<double>((size_t)ninst * 6);
+    s->hslot = A.take<sphg::HeaderSlot>(1);
     if (s->opt.track_ids) {
       s->idsA = A.take<int32_t>(N);
       s->idsB = A.take<int32_t>(N);
@@ -569,10 +585,7 @@ sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int
   int bits = 1;
   while (bits < 32 && ((uint64_t)1 << bits) < L.keys) ++bits;
   s->key_bits = bits;
-  if (s->gexec) {  // grid sizes depend on the layout
-    cudaGraphExecDestroy(s->gexec);
-    s->gexec = nullptr;
-  }
+  s->drop_graphs();  // grid sizes depend on the layout
   // instance of the first slot of every 256-slot block
   const int64_t blocks = (s->n >> sphg::kInstTabShift) + 1;
   s->hinst_tab.assign((size_t)blocks, 0);
@@ -595,7 +608,7 @@ sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int
 
 sphg_status destroy_impl(sphg_sim* s) {
   if (!s) return SPHG_OK;
-  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  s->drop_graphs();
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   if (s->cap_stream2) cudaStreamDestroy(s->cap_stream2);
   if (s->arena.base) cudaFree(s->arena.base);
@@ -707,6 +720,7 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
       !host_stage(s, (size_t)s->n * (sizeof(float2) * 2 + sizeof(float4) + sizeof(float) + sizeof(uint32_t))))
     st = fail(SPHG_OOM, "pinned host staging");
   if (st == SPHG_OK && s->n > 0 && s->opt.use_graph) st = build_graph(s);
+  if (st == SPHG_OK && s->n > 0 && s->opt.use_graph) st = build_graph(s, true);  // with step headers
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;
@@ -932,22 +946,76 @@ sphg_status sphg_set_dt(sphg_sim* s, int32_t inst, double dt) {
   }
   if (s->ninst > 0)
     SPHG_CUDA(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * s->ninst, cudaMemcpyHostToDevice));
-  if (s->gexec) {  // the single-instance descriptor is a kernel argument of the captured graph
-    cudaGraphExecDestroy(s->gexec);
-    s->gexec = nullptr;
-  }
+  s->drop_graphs();  // the single-instance descriptor is a kernel argument of the captured graphs
   return SPHG_OK;
+}
+
+// A pointer through which kernels write the caller's array `out`, or null when
+// they cannot (the values are then copied): device or managed memory, pinned
+// host memory (mapped under unified addressing), or -- when host access is on
+// and the device reads and writes pageable memory -- the array itself.
+static double* device_view(sphg_sim* s, double* out) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, out) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return out;
+  if (at.type == cudaMemoryTypeHost) return static_cast<double*>(at.devicePointer);
+  return s->host_direct ? out : nullptr;  // host_direct is set only where pageable access works
+}
+
+static int diag_chunk_count(const sphg_sim* s) {
+  int64_t max_n = 0;
+  for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
+  return sphg::diag_chunks(max_n, s->diag_chunks);
 }
 
 sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream) {
   if (!s || !out) return fail(SPHG_INVALID_ARG, "null argument");
   if (!s->preloop_done) return fail(SPHG_INVALID_ARG, "no computed state");
   cudaStream_t st = (cudaStream_t)stream;
-  int64_t max_n = 0;
-  for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
-  const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
-  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, s->diag_out, st));
-  SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst, cudaMemcpyDeviceToHost, st));
+  const int chunks = diag_chunk_count(s);
+  double* dv = device_view(s, out);
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, dv ? dv : s->diag_out,
+                                     st));
+  if (!dv) SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst, cudaMemcpyDeviceToHost, st));
+  return SPHG_OK;
+}
+
+sphg_status sphg_stream_synchronize(void* stream) {
+  SPHG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return SPHG_OK;
+}
+
+sphg_status sphg_step_headers(sphg_sim* s, int64_t nsteps, double* out, void* stream) {
+  if (!s || !s->preloop_done) return fail(SPHG_INVALID_ARG, "run sphg_preloop before sphg_step_headers");
+  if (nsteps < 0) return fail(SPHG_INVALID_ARG, "nsteps < 0");
+  if (nsteps == 0) return SPHG_OK;
+  if (!out) return fail(SPHG_INVALID_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t per = (size_t)6 * s->ninst;
+  double* dv = s->n > 0 ? device_view(s, out) : nullptr;
+  if (!dv) {  // one copy per step
+    const int chunks = diag_chunk_count(s);
+    for (int64_t k = 0; k < nsteps; ++k) {
+      SPHG_TRY(run_steps(s, 1, st));
+      SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, s->diag_out, st));
+      SPHG_CUDA(cudaMemcpyAsync(out + per * k, s->diag_out, sizeof(double) * per, cudaMemcpyDeviceToHost, st));
+    }
+    return SPHG_OK;
+  }
+  const sphg::HeaderSlot h = {dv, 0u, 0u};
+  SPHG_CUDA(cudaMemcpyAsync(s->hslot, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  if (s->opt.use_graph) {
+    SPHG_TRY(build_graph(s, true));
+    for (int64_t k = 0; k < nsteps; ++k) SPHG_CUDA(cudaGraphLaunch(s->gexec_hdr, st));
+  } else {
+    for (int64_t k = 0; k < nsteps; ++k) {
+      SPHG_TRY(enqueue_step(s, st));
+      SPHG_TRY(enqueue_header(s, st));
+    }
+  }
   return SPHG_OK;
 }
 

@@ -57,6 +57,7 @@ struct sphg_sim {
   uint4* ranges = nullptr;
   int32_t *idsA = nullptr, *idsB = nullptr;
   double *diag_partials = nullptr, *diag_out = nullptr;
+  sphg::HeaderSlot* hslot = nullptr;  // step headers written into the caller's array
   uint2* tile_ranges = nullptr;
   uint32_t* tile_list = nullptr;
   uint32_t *nbr = nullptr, *ncount = nullptr;
@@ -89,6 +90,12 @@ struct sphg_sim {
   cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;
   bool cond_graph = true;       // full sort under a conditional graph node (when the merge is on)
   cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec_hdr = nullptr;  // the same followed by the step header into hslot
+  void drop_graphs() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (gexec_hdr) cudaGraphExecDestroy(gexec_hdr);
+    gexec = gexec_hdr = nullptr;
+  }
 
   StepArgs args() const {
     StepArgs a;

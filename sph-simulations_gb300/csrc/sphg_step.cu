@@ -436,35 +436,10 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
 // ---------------------------------------------------------------- diagnostics
 constexpr int kDiagThreads = 256;
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
   return v;
-}
-
-// Per (chunk, instance) block: FP64 partial sums of one contiguous piece of the
-// instance, a fixed-shape block reduction (deterministic for a given chunk count).
-__device__ __forceinline__ void block_reduce6(double (&v)[6], double (*sh)[kDiagThreads / 32]) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int f = 0; f < 6; ++f) v[f] = (f == 1) ? warp_max(v[f]) : warp_sum(v[f]);
-  if (lane == 0) {
-#pragma unroll
-    for (int f = 0; f < 6; ++f) sh[f][w] = v[f];
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    const int f = threadIdx.x;
-    double acc = sh[f][0];
-    for (int k = 1; k < kDiagThreads / 32; ++k) acc = (f == 1) ? fmax(acc, sh[f][k]) : acc + sh[f][k];
-    sh[f][0] = acc;
-  }
-  __syncthreads();
 }
 
 // Float-float arithmetic (Knuth's TwoSum, Dekker's Fast2Sum, products split
@@ -487,15 +462,81 @@ struct FFSum {
     c = __fadd_rn(c, __fadd_rn(e, err));
   }
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+  // the sum over a warp, still in float-float (lane 0 holds it)
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+      float t, e;
+      two_sum(s, s2, t, e);
+      s = t;
+      c = __fadd_rn(c, __fadd_rn(c2, e));
+    }
+  }
 };
 
 // Per (chunk, instance) block.  The conservation sums (kinetic energy,
 // momentum) and max |v|^2 carry the FP32 velocities' exact squares in
-// float-float per thread and are reduced in FP64 across threads and blocks;
-// the in-domain count is decided in FP32 and redone in FP64 (out of line)
-// only within a thin band of a wall; counts are integers.
+// float-float (FP32 pipes) through the whole reduction -- per thread, across a
+// warp, the block, and the chunks -- and become FP64 only in the six final
+// values; the in-domain count is decided in FP32 and redone in FP64 (out of
+// line) only within a thin band of a wall; counts are integers.  Every
+// reduction has a fixed shape, so the values are deterministic.
 static __device__ __noinline__ bool inside_d(double x, double y, double lox, double hix, double loy, double hiy) {
   return !(x < lox || x > hix) && !(y < loy || y > hiy);
+}
+
+// One chunk's (or one warp's) partial: three float-float sums, the largest
+// |v|^2 as a normalised float-float pair, two counts.  48 bytes, the size of
+// six doubles per chunk of the partials buffer.
+struct DiagPart {
+  FFSum e2, mx, my;
+  float mh, ml;
+  uint32_t inside, bad, pad0, pad1;
+};
+static_assert(sizeof(DiagPart) == 6 * sizeof(double), "a chunk's slot of the partials buffer");
+
+__device__ __forceinline__ void ff_add(FFSum& a, const FFSum& b) {  // a += b
+  float t, e;
+  two_sum(a.s, b.s, t, e);
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(b.c, e));
+}
+__device__ __forceinline__ void part_add(DiagPart& a, const DiagPart& b) {
+  ff_add(a.e2, b.e2);
+  ff_add(a.mx, b.mx);
+  ff_add(a.my, b.my);
+  if (b.mh > a.mh || (b.mh == a.mh && b.ml > a.ml)) {
+    a.mh = b.mh;
+    a.ml = b.ml;
+  }
+  a.inside += b.inside;
+  a.bad += b.bad;
+}
+__device__ __forceinline__ DiagPart part_shfl_down(const DiagPart& a, int o) {
+  DiagPart b;
+  b.e2.s = __shfl_down_sync(0xffffffffu, a.e2.s, o);
+  b.e2.c = __shfl_down_sync(0xffffffffu, a.e2.c, o);
+  b.mx.s = __shfl_down_sync(0xffffffffu, a.mx.s, o);
+  b.mx.c = __shfl_down_sync(0xffffffffu, a.mx.c, o);
+  b.my.s = __shfl_down_sync(0xffffffffu, a.my.s, o);
+  b.my.c = __shfl_down_sync(0xffffffffu, a.my.c, o);
+  b.mh = __shfl_down_sync(0xffffffffu, a.mh, o);
+  b.ml = __shfl_down_sync(0xffffffffu, a.ml, o);
+  b.inside = __shfl_down_sync(0xffffffffu, a.inside, o);
+  b.bad = __shfl_down_sync(0xffffffffu, a.bad, o);
+  return b;
+}
+// The block's sum in thread 0 (fixed shape: lanes by halving, then the warps in order).
+__device__ __forceinline__ DiagPart part_block_reduce(DiagPart v, DiagPart* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part_add(v, part_shfl_down(v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 1; k < kDiagThreads / 32; ++k) part_add(v, sh[k]);
+  return v;
 }
 
 template <int PREC>
@@ -507,41 +548,49 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
   const int64_t per = (cnt + chunks - 1) / chunks;
   const int64_t b = d.begin + per * blockIdx.x;
   const int64_t e = min((int64_t)d.end, b + per);
-  // Per-thread float-float accumulators (the products of the FP32 velocities are
-  // kept exactly as value + error): FP32 pipes for the elements, FP64 from the
-  // block reduction on.
-  FFSum s2, sx, sy;
-  float mh = 0.f, ml = 0.f;  // largest |v|^2 as a normalised float-float pair
-  int inside = 0, bad = 0;
-  const float band = 1.0e-6f * fmaxf(fabsf(d.hi_x - d.lo_x), fabsf(d.hi_y - d.lo_y));
+  // the instance constants used per particle, in registers
+  const float lo_x = d.lo_x, hi_x = d.hi_x, lo_y = d.lo_y, hi_y = d.hi_y;
+  const float cs_x = d.cs_x, cs_y = d.cs_y, Lx = d.Lx, Ly = d.Ly;
+  const uint32_t cell_base = d.cell_base;
+  const int order = d.order, nx = d.nx;
+  const float band = 1.0e-6f * fmaxf(fabsf(hi_x - lo_x), fabsf(hi_y - lo_y));
+  DiagPart v = {};
   for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const float4 vel = a.velpA[i];
     const float2 p = a.posA[i];
+    const float rho = a.rho[i];
     const float p1 = vel.x * vel.x, e1 = fmaf(vel.x, vel.x, -p1);
     const float p2 = vel.y * vel.y, e2 = fmaf(vel.y, vel.y, -p2);
-    s2.add(p1, e1);
-    s2.add(p2, e2);
-    sx.add(vel.x, 0.f);
-    sy.add(vel.y, 0.f);
+    v.e2.add(p1, e1);
+    v.e2.add(p2, e2);
+    v.mx.add(vel.x, 0.f);
+    v.my.add(vel.y, 0.f);
     float h, l;
     two_sum(p1, p2, h, l);
     l += e1 + e2;
     fast_two_sum(h, l, h, l);
-    if (h > mh || (h == mh && l > ml)) {
-      mh = h;
-      ml = l;
+    if (h > v.mh || (h == v.mh && l > v.ml)) {
+      v.mh = h;
+      v.ml = l;
     }
     int cx = 0, cy = 0;
-    float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
-    float lox = d.lo_x, hix = d.hi_x, loy = d.lo_y, hiy = d.hi_y;
+    const float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
+    float lox = lo_x, hix = hi_x, loy = lo_y, hiy = hi_y;
     if (PREC == 1) {
-      decode_code(d, a.keyA[i] - d.cell_base, cx, cy);
-      lox = -(float)cx * d.cs_x;  // the walls in the cell's frame
-      hix = d.Lx - (float)cx * d.cs_x;
-      loy = -(float)cy * d.cs_y;
-      hiy = d.Ly - (float)cy * d.cs_y;
+      const uint32_t code = a.keyA[i] - cell_base;
+      if (order == 0) {
+        cx = (int)compact1by1(code);
+        cy = (int)compact1by1(code >> 1);
+      } else {
+        cx = (int)(code % (uint32_t)nx);
+        cy = (int)(code / (uint32_t)nx);
+      }
+      lox = -(float)cx * cs_x;  // the walls in the cell's frame
+      hix = Lx - (float)cx * cs_x;
+      loy = -(float)cy * cs_y;
+      hiy = Ly - (float)cy * cs_y;
     }
-    const bool fin = isfinite(x) && isfinite(y) && isfinite(vel.x) && isfinite(vel.y) && isfinite(a.rho[i]);
+    const bool fin = isfinite(x) && isfinite(y) && isfinite(vel.x) && isfinite(vel.y) && isfinite(rho);
     bool in = fin && x >= lox && x <= hix && y >= loy && y <= hiy;
     const bool near = fin && (fabsf(x - lox) <= band || fabsf(x - hix) <= band || fabsf(y - loy) <= band ||
                               fabsf(y - hiy) <= band);
@@ -550,29 +599,58 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
       const double yd = PREC == 1 ? d.lo_yd + cy * d.cs_yd + (double)y : (double)y;
       in = inside_d(xd, yd, d.lo_xd, d.hi_xd, d.lo_yd, d.hi_yd);
     }
-    inside += in ? 1 : 0;
-    bad += fin ? 0 : 1;
+    v.inside += in ? 1u : 0u;
+    v.bad += fin ? 0u : 1u;
   }
-  double v[6] = {0.5 * d.mass_d * s2.value(), (double)mh + (double)ml, (double)inside, d.mass_d * sx.value(),
-                 d.mass_d * sy.value(), (double)bad};
-  __shared__ double sh[6][kDiagThreads / 32];
-  block_reduce6(v, sh);
-  if (threadIdx.x < 6) partials[((size_t)inst * chunks + blockIdx.x) * 6 + threadIdx.x] = sh[threadIdx.x][0];
+  __shared__ DiagPart sh[kDiagThreads / 32];
+  v = part_block_reduce(v, sh);
+  if (threadIdx.x == 0) reinterpret_cast<DiagPart*>(partials)[(size_t)inst * chunks + blockIdx.x] = v;
 }
 
-// One block per instance: strided partials per thread, then the same fixed-shape reduction.
-__global__ void __launch_bounds__(kDiagThreads) step_diag_final(int chunks, const double* partials,
-                                                                double* out) {
+// One block per instance: the chunks' partials strided over the threads, the
+// same fixed-shape reduction, and the six FP64 values
+// {E_k, max |v|^2, N inside, m sum vx, m sum vy, non-finite count}.
+__device__ __forceinline__ bool diag_final_values(const StepArgs& a, int chunks, const double* partials,
+                                                  double (&r)[6]) {
   const int inst = blockIdx.x;
-  double v[6] = {0, 0, 0, 0, 0, 0};
-  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
-    const double* p = partials + ((size_t)inst * chunks + c) * 6;
-#pragma unroll
-    for (int f = 0; f < 6; ++f) v[f] = (f == 1) ? fmax(v[f], p[f]) : v[f] + p[f];
+  const DiagPart* parts = reinterpret_cast<const DiagPart*>(partials) + (size_t)inst * chunks;
+  DiagPart v = {};
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) part_add(v, parts[c]);
+  __shared__ DiagPart sh[kDiagThreads / 32];
+  v = part_block_reduce(v, sh);
+  if (threadIdx.x != 0) return false;
+  const double m = (a.ninst == 1) ? a.d0.mass_d : a.desc[inst].mass_d;
+  r[0] = 0.5 * m * v.e2.value();
+  r[1] = (double)v.mh + (double)v.ml;
+  r[2] = (double)v.inside;
+  r[3] = m * v.mx.value();
+  r[4] = m * v.my.value();
+  r[5] = (double)v.bad;
+  return true;
+}
+
+__global__ void __launch_bounds__(kDiagThreads) step_diag_final(StepArgs a, int chunks, const double* partials,
+                                                                double* out) {
+  double r[6];
+  if (diag_final_values(a, chunks, partials, r))
+    for (int f = 0; f < 6; ++f) out[blockIdx.x * 6 + f] = r[f];
+}
+
+// The same into the step-header slot; the last instance block to finish
+// advances the slot's step index (every block has read it by then).
+__global__ void __launch_bounds__(kDiagThreads) step_diag_final_slot(StepArgs a, int chunks, const double* partials,
+                                                                     HeaderSlot* slot) {
+  double r[6];
+  if (diag_final_values(a, chunks, partials, r)) {
+    const size_t k = *(volatile uint32_t*)&slot->k;
+    for (int f = 0; f < 6; ++f) slot->out[(k * gridDim.x + blockIdx.x) * 6 + f] = r[f];
+    __threadfence();
+    if (atomicAdd(&slot->done, 1u) == gridDim.x - 1) {
+      slot->done = 0;
+      slot->k += 1;
+      __threadfence();
+    }
   }
-  __shared__ double sh[6][kDiagThreads / 32];
-  block_reduce6(v, sh);
-  if (threadIdx.x < 6) out[inst * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // CFL inputs per (chunk, instance): FP64 maxima of |v|^2 and |a|^2 (a from the
@@ -708,7 +786,16 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
   dim3 g(chunks, a.ninst);
   if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
   else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  step_diag_final<<<a.ninst, kDiagThreads, 0, s>>>(chunks, partials, out);
+  step_diag_final<<<a.ninst, kDiagThreads, 0, s>>>(a, chunks, partials, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, int chunks,
+                                    HeaderSlot* slot, cudaStream_t s) {
+  dim3 g(chunks, a.ninst);
+  if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
+  else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
+  step_diag_final_slot<<<a.ninst, kDiagThreads, 0, s>>>(a, chunks, partials, slot);
   return cudaGetLastError();
 }
 

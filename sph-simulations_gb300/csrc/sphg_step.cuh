@@ -70,6 +70,18 @@ cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int
                                      uint32_t* idx, int64_t cap, cudaStream_t st);
 // Per-instance diagnostics: partial sums per (chunk, instance) then a fixed-order
 // final sum; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx, sum m vy, nonfinite.
+// Where the step headers of sphg_step_headers go: the caller's host array
+// (device-accessible), the index of the next step, and the count of instance
+// blocks done with the current one.
+struct HeaderSlot {
+  double* out;
+  uint32_t k;
+  uint32_t done;
+};
+// Diagnostics of the current state written to slot->out[(k * ninst + inst) * 6 ..],
+// then k advanced (by the last instance block to finish).
+cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, int chunks,
+                                    HeaderSlot* slot, cudaStream_t s);
 cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
                                double* out, cudaStream_t s);
 // Diagnostics chunks of the largest instance (at most cap; the partial buffer

@@ -119,6 +119,10 @@ def lib():
         L.sphg_server_submit_lattice.restype = ctypes.c_int
         L.sphg_diagnostics_async.argtypes = [SP, _vp, _vp]
         L.sphg_diagnostics_async.restype = ctypes.c_int
+        L.sphg_step_headers.argtypes = [SP, ctypes.c_int64, _vp, _vp]
+        L.sphg_step_headers.restype = ctypes.c_int
+        L.sphg_stream_synchronize.argtypes = [_vp]
+        L.sphg_stream_synchronize.restype = ctypes.c_int
         L.sphg_set_host_access.argtypes = [SP, ctypes.c_int32]
         L.sphg_set_host_access.restype = ctypes.c_int
         L.sphg_device_attributes.argtypes = [ctypes.c_int32, _ip]
@@ -227,6 +231,26 @@ class Sim:
 
     def step(self, k=1, stream=None):
         check(lib().sphg_step(self._h, int(k), _stream(stream)))
+
+    def step_headers(self, k, out=None, stream=None):
+        """k iterations, each followed by its step header (the 6 values of
+        diagnostics() per instance).  out: the caller's buffer of k * ninst * 6
+        doubles -- a float64 array, or the address of pinned host memory -- filled
+        in stream order; without it an array is allocated and returned after the
+        stream is synchronised, shaped (k, ninst, 6)."""
+        k = int(k)
+        if out is None:
+            arr = np.empty((k, self.ninst, 6), np.float64)
+            check(lib().sphg_step_headers(self._h, k, arr.ctypes.data_as(_vp), _stream(stream)))
+            check(lib().sphg_stream_synchronize(_stream(stream)))
+            return arr
+        if isinstance(out, np.ndarray):
+            if out.dtype != np.float64 or out.size != k * self.ninst * 6 or not out.flags.c_contiguous:
+                raise ValueError("step_headers: out must be a contiguous float64 array of k * ninst * 6")
+            check(lib().sphg_step_headers(self._h, k, out.ctypes.data_as(_vp), _stream(stream)))
+            return out
+        check(lib().sphg_step_headers(self._h, k, ctypes.c_void_p(int(out)), _stream(stream)))
+        return out
 
     def download(self, forces=True, stream=None, out=None):
         """Current state as FP64 arrays in slot order.  out: optional dict of the

@@ -866,6 +866,58 @@ def test_diagnostics_async_equals_sync():
     sim.close()
 
 
+@pytest.mark.parametrize("case", ["graph-pageable", "graph-pinned", "stream", "copies", "batched"])
+def test_step_headers_equal_step_then_diagnostics(case):
+    """sphg_step_headers = the reference's main loop with a header after every
+    iteration: the same values as sphg_step(1) + sphg_diagnostics per iteration,
+    whether the kernels write the caller's array (pageable or pinned) or the
+    headers are copied (host access off), with and without the step graph."""
+    import torch
+    S = _sphg()
+    x, y, vx, vy = jittered(40, 40, 0.005, seed=31, vel=0.3)
+    kw = dict(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.3, 0.3))
+    opts = S.options(precision=S.SPLIT, use_graph=(case != "stream"))
+    if case == "batched":
+        x2, y2, vx2, vy2 = jittered(30, 20, 0.005, seed=37, vel=0.2)
+        prm = [S.params(**kw), S.params(**kw)]
+        counts = [len(x), len(x2)]
+        x, y, vx, vy = (np.concatenate(p) for p in ((x, x2), (y, y2), (vx, vx2), (vy, vy2)))
+        make = lambda: S.Sim(prm, counts, opts)  # noqa: E731
+    else:
+        make = lambda: S.Sim(S.params(**kw), len(x), opts)  # noqa: E731
+    K = 12
+    a, b = make(), make()
+    for sim in (a, b):
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+    if case == "copies":
+        a.set_host_access(0)
+    if case == "graph-pinned":
+        buf = torch.zeros((K, a.ninst, 6), dtype=torch.float64, pin_memory=True)
+        a.step_headers(K, buf.data_ptr())
+        torch.cuda.synchronize()
+        got = buf.numpy().copy()
+    else:
+        got = a.step_headers(K)
+    ref = []
+    for _ in range(K):
+        b.step(1)
+        ref.append(b.diagnostics())
+    ref = np.array(ref)
+    assert got.shape == ref.shape
+    assert (got == ref).all()
+    assert (ref[:, :, 2] == np.asarray(a.counts)[None, :]).all()  # every particle inside
+    sa, sb = a.download(), b.download()
+    for f in ("x", "y", "vx", "vy", "rho"):
+        assert (sa[f] == sb[f]).all(), f
+    # a second call continues from the state and restarts its own header index
+    got2 = a.step_headers(3)
+    b.step(3)
+    assert (got2[-1] == b.diagnostics()).all()
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("prec", ["plain", "split"])
 def test_particles_outside_the_high_walls(prec):
     """Particles beyond the high walls at upload: their cells clamp to the last
