@@ -325,8 +325,8 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
 sphg_status enqueue_header(sphg_sim* s, cudaStream_t st) {
   int64_t max_n = 0;
   for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
-  SPHG_CUDA(sphg::launch_diagnostics_slot(s->args(), s->opt.precision, s->diag_partials,
-                                          sphg::diag_chunks(max_n, s->diag_chunks), s->hslot, st));
+  SPHG_CUDA(sphg::launch_diagnostics_slot(s->args(), s->opt.precision, s->diag_partials, s->diag_tickets,
+                                          sphg::diag_chunks(max_n, s->ninst, s->diag_chunks), s->hslot, st));
   return SPHG_OK;
 }
 
@@ -521,6 +521,7 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     s->diag_partials = A.take<double>((size_t)ninst * s->diag_chunks * 6);
     s->diag_out = A.take<double>((size_t)ninst * 6);
     s->hslot = A.take<sphg::HeaderSlot>(1);
+    s->diag_tickets = A.take<uint32_t>(ninst);
     if (s->opt.track_ids) {
       s->idsA = A.take<int32_t>(N);
       s->idsB = A.take<int32_t>(N);
@@ -702,7 +703,7 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
     delete s;
     return st;
   }
-  st = alloc_arena(s, (size_t)std::max<int64_t>(L.n, 1), L.keys, ninst, sphg::diag_chunks(L.max_n));
+  st = alloc_arena(s, (size_t)std::max<int64_t>(L.n, 1), L.keys, ninst, sphg::diag_chunks(L.max_n, ninst));
   if (st != SPHG_OK) {
     delete s;
     return st;
@@ -901,8 +902,8 @@ sphg_status sphg_diagnostics(sphg_sim* s, double* out, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   int64_t max_n = 0;
   for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
-  const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
-  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks,
+  const int chunks = sphg::diag_chunks(max_n, s->ninst, s->diag_chunks);
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, s->diag_tickets, chunks,
                                      s->diag_out, st));
   SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst,
                             cudaMemcpyDeviceToHost, st));
@@ -918,7 +919,7 @@ sphg_status sphg_cfl_dt(sphg_sim* s, double cfl, double force_coef, double* out,
     SPHG_CUDA(sphg::launch_force(s->args(), s->opt.precision, sphg::kForceOnly, st));
     int64_t max_n = 0;
     for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
-    const int chunks = sphg::diag_chunks(max_n, s->diag_chunks);
+    const int chunks = sphg::diag_chunks(max_n, s->ninst, s->diag_chunks);
     SPHG_CUDA(sphg::launch_cfl(s->args(), s->diag_partials, chunks, s->diag_out, st));
   }
   std::vector<double> m((size_t)6 * s->ninst, 0.0);
@@ -968,7 +969,7 @@ static double* device_view(sphg_sim* s, double* out) {
 static int diag_chunk_count(const sphg_sim* s) {
   int64_t max_n = 0;
   for (const InstDesc& d : s->hdesc) max_n = std::max<int64_t>(max_n, d.end - d.begin);
-  return sphg::diag_chunks(max_n, s->diag_chunks);
+  return sphg::diag_chunks(max_n, s->ninst, s->diag_chunks);
 }
 
 sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream) {
@@ -977,7 +978,7 @@ sphg_status sphg_diagnostics_async(sphg_sim* s, double* out, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   const int chunks = diag_chunk_count(s);
   double* dv = device_view(s, out);
-  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, dv ? dv : s->diag_out,
+  SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, s->diag_tickets, chunks, dv ? dv : s->diag_out,
                                      st));
   if (!dv) SPHG_CUDA(cudaMemcpyAsync(out, s->diag_out, sizeof(double) * 6 * s->ninst, cudaMemcpyDeviceToHost, st));
   return SPHG_OK;
@@ -1000,7 +1001,7 @@ sphg_status sphg_step_headers(sphg_sim* s, int64_t nsteps, double* out, void* st
     const int chunks = diag_chunk_count(s);
     for (int64_t k = 0; k < nsteps; ++k) {
       SPHG_TRY(run_steps(s, 1, st));
-      SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, chunks, s->diag_out, st));
+      SPHG_CUDA(sphg::launch_diagnostics(s->args(), s->opt.precision, s->diag_partials, s->diag_tickets, chunks, s->diag_out, st));
       SPHG_CUDA(cudaMemcpyAsync(out + per * k, s->diag_out, sizeof(double) * per, cudaMemcpyDeviceToHost, st));
     }
     return SPHG_OK;

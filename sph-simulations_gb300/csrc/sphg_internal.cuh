@@ -57,6 +57,7 @@ struct sphg_sim {
   uint4* ranges = nullptr;
   int32_t *idsA = nullptr, *idsB = nullptr;
   double *diag_partials = nullptr, *diag_out = nullptr;
+  uint32_t* diag_tickets = nullptr;  // per instance: chunks done in the running diagnostics launch
   sphg::HeaderSlot* hslot = nullptr;  // step headers written into the caller's array
   uint2* tile_ranges = nullptr;
   uint32_t* tile_list = nullptr;

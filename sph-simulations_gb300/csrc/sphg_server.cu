@@ -322,7 +322,7 @@ sphg_status sphg_server_create(double hbm_budget_bytes, int32_t max_instances, c
   cap_n = std::min(cap_n, ((size_t)1 << 27) - 1);
   uint64_t cap_keys = (uint64_t)std::floor(0.5 * hbm_budget_bytes / 16.0);
   cap_keys = std::min<uint64_t>(cap_keys, 0xffffff00ull);
-  const int chunks = sphg::diag_chunks((int64_t)cap_n, 64);
+  const int chunks = sphg::diag_chunks((int64_t)cap_n, max_instances, 64);
   st = alloc_arena(sim, std::max<size_t>(cap_n, 1), cap_keys, max_instances, chunks);
   if (st == SPHG_OK) {
     if (cudaMallocHost((void**)&s->htab, sizeof(RepackEntry) * max_instances) != cudaSuccess ||

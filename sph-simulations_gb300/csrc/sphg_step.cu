@@ -435,6 +435,7 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
 
 // ---------------------------------------------------------------- diagnostics
 constexpr int kDiagThreads = 256;
+constexpr int kDiagBatch = 4;
 
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
@@ -539,9 +540,24 @@ __device__ __forceinline__ DiagPart part_block_reduce(DiagPart v, DiagPart* sh) 
   return v;
 }
 
-template <int PREC>
-__global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, int chunks,
-                                                                  double* partials) {
+// A partial written by another block of this launch (past L1).
+__device__ __forceinline__ DiagPart load_part(const DiagPart* p) {
+  const uint4* q = reinterpret_cast<const uint4*>(p);
+  uint4 w[3] = {__ldcg(q), __ldcg(q + 1), __ldcg(q + 2)};
+  DiagPart r;
+  memcpy(&r, w, sizeof(r));
+  return r;
+}
+
+// One launch: every (chunk, instance) block reduces its particles into a
+// partial; the last block of an instance to finish (a ticket counter, reset
+// by it for the next launch) reduces the instance's partials into its six
+// FP64 values {E_k, max |v|^2, N inside, m sum vx, m sum vy, non-finite
+// count}, written to out[inst * 6 ..] or, with a header slot, to the slot's
+// array at step k -- whose index the last instance to finish then advances.
+template <int PREC, bool SLOT>
+__global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks, double* partials,
+                                                          uint32_t* tickets, double* out, HeaderSlot* slot) {
   const int inst = blockIdx.y;
   const InstDesc& d = (a.ninst == 1) ? a.d0 : a.desc[inst];
   const int64_t cnt = d.end - d.begin;
@@ -555,101 +571,104 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag_partial(StepArgs a, in
   const int order = d.order, nx = d.nx;
   const float band = 1.0e-6f * fmaxf(fabsf(hi_x - lo_x), fabsf(hi_y - lo_y));
   DiagPart v = {};
-  for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-    const float4 vel = a.velpA[i];
-    const float2 p = a.posA[i];
-    const float rho = a.rho[i];
-    const float p1 = vel.x * vel.x, e1 = fmaf(vel.x, vel.x, -p1);
-    const float p2 = vel.y * vel.y, e2 = fmaf(vel.y, vel.y, -p2);
-    v.e2.add(p1, e1);
-    v.e2.add(p2, e2);
-    v.mx.add(vel.x, 0.f);
-    v.my.add(vel.y, 0.f);
-    float h, l;
-    two_sum(p1, p2, h, l);
-    l += e1 + e2;
-    fast_two_sum(h, l, h, l);
-    if (h > v.mh || (h == v.mh && l > v.ml)) {
-      v.mh = h;
-      v.ml = l;
+  // kDiagBatch particles per thread at a time: all their loads are issued
+  // before any of them is used (the rare FP64 wall test is an out-of-line call
+  // the compiler cannot move loads across)
+  for (int64_t i0 = b + threadIdx.x; i0 < e; i0 += (int64_t)kDiagBatch * blockDim.x) {
+    float4 vb[kDiagBatch];
+    float2 pb[kDiagBatch];
+    float rb[kDiagBatch];
+    uint32_t kb[kDiagBatch];
+#pragma unroll
+    for (int u = 0; u < kDiagBatch; ++u) {
+      const int64_t i = i0 + (int64_t)u * blockDim.x;
+      const bool ok = i < e;
+      vb[u] = ok ? a.velpA[i] : make_float4(0.f, 0.f, 0.f, 1.f);
+      pb[u] = ok ? a.posA[i] : make_float2(0.5f * (lo_x + hi_x), 0.5f * (lo_y + hi_y));
+      rb[u] = ok ? a.rho[i] : 1.f;
+      kb[u] = (PREC == 1 && ok) ? a.keyA[i] : cell_base;
     }
-    int cx = 0, cy = 0;
-    const float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
-    float lox = lo_x, hix = hi_x, loy = lo_y, hiy = hi_y;
-    if (PREC == 1) {
-      const uint32_t code = a.keyA[i] - cell_base;
-      if (order == 0) {
-        cx = (int)compact1by1(code);
-        cy = (int)compact1by1(code >> 1);
-      } else {
-        cx = (int)(code % (uint32_t)nx);
-        cy = (int)(code / (uint32_t)nx);
+#pragma unroll
+    for (int u = 0; u < kDiagBatch; ++u) {
+      if (i0 + (int64_t)u * blockDim.x >= e) break;
+      const float4 vel = vb[u];
+      const float2 p = pb[u];
+      const float rho = rb[u];
+      const float p1 = vel.x * vel.x, e1 = fmaf(vel.x, vel.x, -p1);
+      const float p2 = vel.y * vel.y, e2 = fmaf(vel.y, vel.y, -p2);
+      v.e2.add(p1, e1);
+      v.e2.add(p2, e2);
+      v.mx.add(vel.x, 0.f);
+      v.my.add(vel.y, 0.f);
+      float h, l;
+      two_sum(p1, p2, h, l);
+      l += e1 + e2;
+      fast_two_sum(h, l, h, l);
+      if (h > v.mh || (h == v.mh && l > v.ml)) {
+        v.mh = h;
+        v.ml = l;
       }
-      lox = -(float)cx * cs_x;  // the walls in the cell's frame
-      hix = Lx - (float)cx * cs_x;
-      loy = -(float)cy * cs_y;
-      hiy = Ly - (float)cy * cs_y;
+      int cx = 0, cy = 0;
+      const float x = p.x, y = p.y;  // position, or offset in cell (cx, cy)
+      float lox = lo_x, hix = hi_x, loy = lo_y, hiy = hi_y;
+      if (PREC == 1) {
+        const uint32_t code = kb[u] - cell_base;
+        if (order == 0) {
+          cx = (int)compact1by1(code);
+          cy = (int)compact1by1(code >> 1);
+        } else {
+          cx = (int)(code % (uint32_t)nx);
+          cy = (int)(code / (uint32_t)nx);
+        }
+        lox = -(float)cx * cs_x;  // the walls in the cell's frame
+        hix = Lx - (float)cx * cs_x;
+        loy = -(float)cy * cs_y;
+        hiy = Ly - (float)cy * cs_y;
+      }
+      const bool fin = isfinite(x) && isfinite(y) && isfinite(vel.x) && isfinite(vel.y) && isfinite(rho);
+      bool in = fin && x >= lox && x <= hix && y >= loy && y <= hiy;
+      const bool near = fin && (fabsf(x - lox) <= band || fabsf(x - hix) <= band || fabsf(y - loy) <= band ||
+                                fabsf(y - hiy) <= band);
+      if (near) {
+        const double xd = PREC == 1 ? d.lo_xd + cx * d.cs_xd + (double)x : (double)x;
+        const double yd = PREC == 1 ? d.lo_yd + cy * d.cs_yd + (double)y : (double)y;
+        in = inside_d(xd, yd, d.lo_xd, d.hi_xd, d.lo_yd, d.hi_yd);
+      }
+      v.inside += in ? 1u : 0u;
+      v.bad += fin ? 0u : 1u;
     }
-    const bool fin = isfinite(x) && isfinite(y) && isfinite(vel.x) && isfinite(vel.y) && isfinite(rho);
-    bool in = fin && x >= lox && x <= hix && y >= loy && y <= hiy;
-    const bool near = fin && (fabsf(x - lox) <= band || fabsf(x - hix) <= band || fabsf(y - loy) <= band ||
-                              fabsf(y - hiy) <= band);
-    if (near) {
-      const double xd = PREC == 1 ? d.lo_xd + cx * d.cs_xd + (double)x : (double)x;
-      const double yd = PREC == 1 ? d.lo_yd + cy * d.cs_yd + (double)y : (double)y;
-      in = inside_d(xd, yd, d.lo_xd, d.hi_xd, d.lo_yd, d.hi_yd);
-    }
-    v.inside += in ? 1u : 0u;
-    v.bad += fin ? 0u : 1u;
   }
   __shared__ DiagPart sh[kDiagThreads / 32];
+  __shared__ bool last;
   v = part_block_reduce(v, sh);
-  if (threadIdx.x == 0) reinterpret_cast<DiagPart*>(partials)[(size_t)inst * chunks + blockIdx.x] = v;
-}
-
-// One block per instance: the chunks' partials strided over the threads, the
-// same fixed-shape reduction, and the six FP64 values
-// {E_k, max |v|^2, N inside, m sum vx, m sum vy, non-finite count}.
-__device__ __forceinline__ bool diag_final_values(const StepArgs& a, int chunks, const double* partials,
-                                                  double (&r)[6]) {
-  const int inst = blockIdx.x;
-  const DiagPart* parts = reinterpret_cast<const DiagPart*>(partials) + (size_t)inst * chunks;
-  DiagPart v = {};
-  for (int c = threadIdx.x; c < chunks; c += blockDim.x) part_add(v, parts[c]);
-  __shared__ DiagPart sh[kDiagThreads / 32];
-  v = part_block_reduce(v, sh);
-  if (threadIdx.x != 0) return false;
-  const double m = (a.ninst == 1) ? a.d0.mass_d : a.desc[inst].mass_d;
-  r[0] = 0.5 * m * v.e2.value();
-  r[1] = (double)v.mh + (double)v.ml;
-  r[2] = (double)v.inside;
-  r[3] = m * v.mx.value();
-  r[4] = m * v.my.value();
-  r[5] = (double)v.bad;
-  return true;
-}
-
-__global__ void __launch_bounds__(kDiagThreads) step_diag_final(StepArgs a, int chunks, const double* partials,
-                                                                double* out) {
-  double r[6];
-  if (diag_final_values(a, chunks, partials, r))
-    for (int f = 0; f < 6; ++f) out[blockIdx.x * 6 + f] = r[f];
-}
-
-// The same into the step-header slot; the last instance block to finish
-// advances the slot's step index (every block has read it by then).
-__global__ void __launch_bounds__(kDiagThreads) step_diag_final_slot(StepArgs a, int chunks, const double* partials,
-                                                                     HeaderSlot* slot) {
-  double r[6];
-  if (diag_final_values(a, chunks, partials, r)) {
-    const size_t k = *(volatile uint32_t*)&slot->k;
-    for (int f = 0; f < 6; ++f) slot->out[(k * gridDim.x + blockIdx.x) * 6 + f] = r[f];
+  DiagPart* parts = reinterpret_cast<DiagPart*>(partials) + (size_t)inst * chunks;
+  if (threadIdx.x == 0) {
+    parts[blockIdx.x] = v;
     __threadfence();
-    if (atomicAdd(&slot->done, 1u) == gridDim.x - 1) {
-      slot->done = 0;
-      slot->k += 1;
-      __threadfence();
-    }
+    last = atomicAdd(tickets + inst, 1u) == (uint32_t)chunks - 1u;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  DiagPart f = {};
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) part_add(f, load_part(parts + c));
+  f = part_block_reduce(f, sh);
+  if (threadIdx.x != 0) return;
+  tickets[inst] = 0;
+  const double m = d.mass_d;
+  const double r[6] = {0.5 * m * f.e2.value(), (double)f.mh + (double)f.ml, (double)f.inside, m * f.mx.value(),
+                       m * f.my.value(), (double)f.bad};
+  if (!SLOT) {
+    for (int q = 0; q < 6; ++q) out[inst * 6 + q] = r[q];
+    return;
+  }
+  const size_t k = *(volatile uint32_t*)&slot->k;
+  for (int q = 0; q < 6; ++q) slot->out[(k * gridDim.y + inst) * 6 + q] = r[q];
+  __threadfence();
+  if (atomicAdd(&slot->done, 1u) == gridDim.y - 1) {
+    slot->done = 0;
+    slot->k += 1;
+    __threadfence();
   }
 }
 
@@ -774,28 +793,27 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
   return cudaGetLastError();
 }
 
-int diag_chunks(int64_t max_inst_n, int cap) {
-  int64_t c = (max_inst_n + 1023) / 1024;  // about four particles per thread
+int diag_chunks(int64_t max_inst_n, int ninst, int cap) {
+  const int64_t per = ninst > 1 ? 1024 : 4096;  // sixteen particles per thread for a single instance
+  int64_t c = (max_inst_n + per - 1) / per;
   if (c < 1) c = 1;
   if (c > cap) c = cap;
   return (int)c;
 }
 
-cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
+cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, uint32_t* tickets, int chunks,
                                double* out, cudaStream_t s) {
   dim3 g(chunks, a.ninst);
-  if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  step_diag_final<<<a.ninst, kDiagThreads, 0, s>>>(a, chunks, partials, out);
+  if (precision) step_diag<1, false><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, out, nullptr);
+  else step_diag<0, false><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, out, nullptr);
   return cudaGetLastError();
 }
 
-cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, int chunks,
-                                    HeaderSlot* slot, cudaStream_t s) {
+cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, uint32_t* tickets,
+                                    int chunks, HeaderSlot* slot, cudaStream_t s) {
   dim3 g(chunks, a.ninst);
-  if (precision) step_diag_partial<1><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  else step_diag_partial<0><<<g, kDiagThreads, 0, s>>>(a, chunks, partials);
-  step_diag_final_slot<<<a.ninst, kDiagThreads, 0, s>>>(a, chunks, partials, slot);
+  if (precision) step_diag<1, true><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, nullptr, slot);
+  else step_diag<0, true><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, nullptr, slot);
   return cudaGetLastError();
 }
 

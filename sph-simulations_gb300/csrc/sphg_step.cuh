@@ -80,13 +80,15 @@ struct HeaderSlot {
 };
 // Diagnostics of the current state written to slot->out[(k * ninst + inst) * 6 ..],
 // then k advanced (by the last instance block to finish).
-cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, int chunks,
-                                    HeaderSlot* slot, cudaStream_t s);
-cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, int chunks,
+cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, uint32_t* tickets,
+                                    int chunks, HeaderSlot* slot, cudaStream_t s);
+// The same into out[inst * 6 ..] (device-accessible).  partials: ninst x chunks
+// x 6 doubles; tickets: ninst counters, zero between launches.
+cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, uint32_t* tickets, int chunks,
                                double* out, cudaStream_t s);
 // Diagnostics chunks of the largest instance (at most cap; the partial buffer
-// holds ninst x cap x 6 doubles).
-int diag_chunks(int64_t max_inst_n, int cap = 1024);
+// holds ninst x chunks x 6 doubles).
+int diag_chunks(int64_t max_inst_n, int ninst, int cap = 4096);
 // out[6*inst + {0, 1}] = max |v|^2, max |a|^2 of each instance (a.acc must hold the forces).
 cudaError_t launch_cfl(const StepArgs& a, double* partials, int chunks, double* out, cudaStream_t s);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
