@@ -482,9 +482,43 @@ int main(int argc, char** argv) {
     if (snap_freq > 0 && steps > 0) snapshot(0);
   }
 
-  // MainLoopComputation
+  // MainLoopComputation.  With a header after every iteration and no per-step
+  // measurement, the iterations up to the next checkpoint or snapshot run as
+  // one sphg_step_headers call (at most kBlock at a time) and their headers
+  // are printed from its array: the same lines in the same order, without a
+  // host synchronisation per iteration.
+  constexpr long long kBlock = 256;
+  std::vector<double> hbuf(6 * kBlock);
+  auto next_multiple = [](long long i, long long f) { return (i + f - 1) / f * f; };
   timers.start("main_loop");
-  for (long long i = first; i < steps; ++i) {
+  for (long long i = first; i < steps;) {
+    long long j = i;  // last iteration of this round
+    if (!measure && header_freq == 1) {
+      j = std::min(steps - 1, i + kBlock - 1);
+      if (ckpt_freq > 0) j = std::min(j, next_multiple(i, ckpt_freq));
+      if (snap_freq > 0) j = std::min(j, next_multiple(i, snap_freq));
+      timers.start("gpu_step");
+      st = sphg_step_headers(sim, j - i + 1, hbuf.data(), nullptr);
+      if (st == SPHG_OK) st = sphg_stream_synchronize(nullptr);
+      timers.stop("gpu_step");
+      if (st != SPHG_OK) die("sphg_step_headers", st);
+      timers.start("IO");
+      for (long long k = i; k < j; ++k) {
+        const double* h = hbuf.data() + 6 * (k - i);
+        std::cout << "Step= " << k << "\t N=" << (long long)h[2] << "\t E_k=" << h[0] << "\t |v|_max=" << h[1]
+                  << std::endl;
+      }
+      timers.stop("IO");
+      if (ckpt_freq > 0 && j % ckpt_freq == 0) {
+        timers.start("IO");
+        checkpoint(j);
+        timers.stop("IO");
+      }
+      header(j);  // also reads the kernels' error words
+      if (snap_freq > 0 && j % snap_freq == 0) snapshot(j);
+      i = j + 1;
+      continue;
+    }
     timers.start("gpu_step");
     st = sphg_step(sim, 1, nullptr);
     timers.stop("gpu_step");
@@ -500,6 +534,7 @@ int main(int argc, char** argv) {
     }
     if (i % header_freq == 0 || i == steps - 1) header(i);
     if (snap_freq > 0 && i % snap_freq == 0) snapshot(i);
+    ++i;
   }
   writer.finish();
   timers.stop("main_loop");
