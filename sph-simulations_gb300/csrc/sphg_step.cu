@@ -17,6 +17,7 @@
 // exactly from FP32 state: the FP32 value decides unless it lies in a thin
 // band around the threshold, where the reference's FP64 expression is
 // evaluated (sphg_common.cuh).
+#include <algorithm>
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -575,7 +576,7 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
   // before any of them is used (the rare FP64 wall test is an out-of-line call
   // the compiler cannot move loads across)
   for (int64_t i0 = b + threadIdx.x; i0 < e; i0 += (int64_t)kDiagBatch * blockDim.x) {
-    float4 vb[kDiagBatch];
+    float2 vb[kDiagBatch];  // (vx, vy) of velpA
     float2 pb[kDiagBatch];
     float rb[kDiagBatch];
     uint32_t kb[kDiagBatch];
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
     for (int u = 0; u < kDiagBatch; ++u) {
       const int64_t i = i0 + (int64_t)u * blockDim.x;
       const bool ok = i < e;
-      vb[u] = ok ? a.velpA[i] : make_float4(0.f, 0.f, 0.f, 1.f);
+      vb[u] = ok ? reinterpret_cast<const float2*>(a.velpA)[2 * i] : make_float2(0.f, 0.f);
       pb[u] = ok ? a.posA[i] : make_float2(0.5f * (lo_x + hi_x), 0.5f * (lo_y + hi_y));
       rb[u] = ok ? a.rho[i] : 1.f;
       kb[u] = (PREC == 1 && ok) ? a.keyA[i] : cell_base;
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
 #pragma unroll
     for (int u = 0; u < kDiagBatch; ++u) {
       if (i0 + (int64_t)u * blockDim.x >= e) break;
-      const float4 vel = vb[u];
+      const float2 vel = vb[u];
       const float2 p = pb[u];
       const float rho = rb[u];
       const float p1 = vel.x * vel.x, e1 = fmaf(vel.x, vel.x, -p1);
@@ -794,8 +795,22 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
 }
 
 int diag_chunks(int64_t max_inst_n, int ninst, int cap) {
-  const int64_t per = ninst > 1 ? 1024 : 4096;  // sixteen particles per thread for a single instance
-  int64_t c = (max_inst_n + per - 1) / per;
+  int64_t c;
+  if (ninst > 1) {
+    c = (max_inst_n + 1023) / 1024;  // about four particles per thread
+  } else {
+    // one instance: two blocks per SM, all resident at once and equally loaded
+    static const int sms = [] {
+      int dev = 0, v = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        v = 152;
+      }
+      return v;
+    }();
+    c = std::min<int64_t>((max_inst_n + 255) / 256, 2 * (int64_t)sms);
+  }
   if (c < 1) c = 1;
   if (c > cap) c = cap;
   return (int)c;
