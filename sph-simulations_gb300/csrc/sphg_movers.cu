@@ -35,6 +35,7 @@ constexpr int kCompactWords = 1;  // words per thread: 256 x 1 word = one group 
 static_assert(kCompactThreads * kCompactWords * 32 == (1 << kGroupShift), "one block per group");
 constexpr int kRankThreads = 256;  // 8 movers per block
 constexpr int kStayThreads = 256;
+constexpr int kMergeSlots = 4;  // slots per thread of movers_merge
 
 __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p, uint32_t m) {
   if (p >= a.n) return m;
@@ -224,50 +225,74 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
   }
 }
 
-// Thread i places slot i if it kept its key (the movers are placed already).
-// A stayer's position is its rank among stayers + the movers ordered before
-// it.  A warp's slots are consecutive, so the movers ordered before any of them
-// lie between the counts of its first and last slot: two interleaved warp-wide
-// searches per warp, then each lane refines inside that (usually empty)
-// interval.  Everything that does not depend on the searches is loaded first.
+// Each block places kMergeSlots x 256 consecutive slots, those that kept their
+// key (the movers are placed already): a stayer's position is its rank among
+// stayers + the movers ordered before it.  The movers ordered before any slot
+// of the block lie between the counts of its first and last slot, found by
+// warp 0 with two interleaved warp-wide searches while the other threads load
+// their slots' state; each thread then refines inside that (usually empty)
+// interval.  Four slots per thread (strided by the block size, so every load
+// and store stays coalesced) keep all blocks resident in one wave.
 __global__ void __launch_bounds__(kStayThreads) movers_merge(MoverArgs a) {
   cudaGridDependencySynchronize();  // the sorted movers of movers_rank_place
   if (!a.ctl[0]) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m = a.ctl[1];
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = i - lane;
-  if (w0 >= a.n) return;  // the whole warp is past the last slot
-  const bool valid = i < a.n;
-  const uint32_t k = valid ? a.keyA[i] : 0xFFFFFFFFu;
-  const uint32_t mw = valid ? a.mask[i >> 5] : 0xFFFFFFFFu;
-  const bool stay = valid && !((mw >> lane) & 1u);
-  uint32_t before = 0;
-  float2 p = make_float2(0.f, 0.f), vel = make_float2(0.f, 0.f);
-  int32_t id = 0;
-  if (stay) {
-    before = a.wprefix[i >> 5] + __popc(mw & ((1u << lane) - 1u));
-    p = a.posB[i];
-    vel = a.velB[i];
-    if (a.idsA) id = a.idsB[i];
+  const int64_t base = (int64_t)blockIdx.x * (kStayThreads * kMergeSlots);
+  if (base >= a.n) return;
+  const int64_t last = min(base + kStayThreads * kMergeSlots, a.n) - 1;
+  __shared__ uint32_t bounds[2];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const unsigned long long v0 = ((unsigned long long)a.keyA[base] << 32) | (uint32_t)base;
+    const unsigned long long v1 = ((unsigned long long)a.keyA[last] << 32) | (uint32_t)last;
+    uint32_t lo, hi;
+    warp_count_below2(a.msorted, m, v0, v1, lane, lo, hi);
+    if (lane == 0) {
+      bounds[0] = lo;
+      bounds[1] = hi;
+    }
   }
-  const int last = (int)(min(w0 + 31, a.n - 1) - w0);
-  const unsigned long long v0 = ((unsigned long long)__shfl_sync(0xffffffffu, k, 0) << 32) | (uint32_t)w0;
-  const unsigned long long v1 =
-      ((unsigned long long)__shfl_sync(0xffffffffu, k, last) << 32) | (uint32_t)(w0 + last);
-  uint32_t wlo, whi;
-  warp_count_below2(a.msorted, m, v0, v1, lane, wlo, whi);
-  if (!stay) return;
-  const unsigned long long v = ((unsigned long long)k << 32) | (uint32_t)i;
-  uint32_t lo = wlo, hi = whi;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (a.msorted[mid] < v) lo = mid + 1;
-    else hi = mid;
+  uint32_t key[kMergeSlots], before[kMergeSlots];
+  float2 p[kMergeSlots], vel[kMergeSlots];
+  int32_t id[kMergeSlots];
+  bool stay[kMergeSlots];
+#pragma unroll
+  for (int u = 0; u < kMergeSlots; ++u) {
+    const int64_t i = base + (int64_t)u * kStayThreads + threadIdx.x;
+    stay[u] = false;
+    key[u] = 0;
+    before[u] = 0;
+    id[u] = 0;
+    p[u] = vel[u] = make_float2(0.f, 0.f);
+    if (i < a.n) {
+      const uint32_t mw = a.mask[i >> 5];
+      stay[u] = !((mw >> (i & 31)) & 1u);
+      if (stay[u]) {
+        key[u] = a.keyA[i];
+        before[u] = a.wprefix[i >> 5] + __popc(mw & ((1u << (i & 31)) - 1u));
+        p[u] = a.posB[i];
+        vel[u] = a.velB[i];
+        if (a.idsA) id[u] = a.idsB[i];
+      }
+    }
   }
-  const int64_t fin = i - (int64_t)before + lo;
-  if (fin >= 0 && fin < a.n) place_values(a, i, fin, k, p, vel, id);
-  else a.ctl[2] = 1u;
+  __syncthreads();
+  const uint32_t blo = bounds[0], bhi = bounds[1];
+#pragma unroll
+  for (int u = 0; u < kMergeSlots; ++u) {
+    if (!stay[u]) continue;
+    const int64_t i = base + (int64_t)u * kStayThreads + threadIdx.x;
+    const unsigned long long v = ((unsigned long long)key[u] << 32) | (uint32_t)i;
+    uint32_t lo = blo, hi = bhi;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (a.msorted[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    const int64_t fin = i - (int64_t)before[u] + lo;
+    if (fin >= 0 && fin < a.n) place_values(a, i, fin, key[u], p[u], vel[u], id[u]);
+    else a.ctl[2] = 1u;
+  }
 }
 
 }  // namespace
@@ -282,8 +307,9 @@ cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st) {
   cudaError_t e = launch_pdl(movers_rank_place, dim3((unsigned)((cap + per_block - 1) / per_block)),
                              dim3(kRankThreads), 0, st, a);
   if (e != cudaSuccess) return e;
-  e = launch_pdl(movers_merge, dim3((unsigned)((a.n + kStayThreads - 1) / kStayThreads)), dim3(kStayThreads), 0,
-                 st, a);
+  const int64_t merge_block = (int64_t)kStayThreads * kMergeSlots;
+  e = launch_pdl(movers_merge, dim3((unsigned)((a.n + merge_block - 1) / merge_block)), dim3(kStayThreads), 0, st,
+                 a);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

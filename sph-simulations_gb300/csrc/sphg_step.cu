@@ -72,12 +72,14 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- reorder + cell ranges
-__global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const uint32_t k = a.keyS[i];
+// kReorderSlots slots per thread, strided by the block size (coalesced), their
+// keys loaded before any is used.
+constexpr int kReorderSlots = 4;
+
+__device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint32_t k, uint32_t kprev,
+                                             uint32_t knext, bool gather, uint32_t ep) {
   a.keyA[i] = k;
-  if (!(a.merged && *a.merged)) {  // gather (after a full sort; a merge scattered the state already)
+  if (gather) {  // after a full sort (a merge scattered the state already)
     const uint32_t src = a.perm[i];
     a.posA[i] = a.posB[src];
     const float2 v = a.velB[src];
@@ -85,11 +87,9 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
     if (a.track_ids) a.idsA[i] = a.idsB[src];
   }
   uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
-  const uint32_t kprev = i > 0 ? a.keyS[i - 1] : kNoIndex;
-  const uint32_t knext = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;
   if (k != kprev) {
     r[4 * (size_t)k] = (uint32_t)i;
-    r[4 * (size_t)k + 2] = *a.epoch;
+    r[4 * (size_t)k + 2] = ep;
   }
   if (k != knext) r[4 * (size_t)k + 1] = (uint32_t)(i + 1);
   if (a.tile_bits) {
@@ -101,6 +101,28 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
       a.tile_list[atomicAdd(a.tile_count, 1u)] = t;
     }
     if (knext == kNoIndex || (knext >> sh) != t) tr[2 * (size_t)t + 1] = (uint32_t)(i + 1);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
+  const int64_t base = (int64_t)blockIdx.x * (kThreads * kReorderSlots) + threadIdx.x;
+  uint32_t k[kReorderSlots], kp[kReorderSlots], kn[kReorderSlots];
+#pragma unroll
+  for (int u = 0; u < kReorderSlots; ++u) {
+    const int64_t i = base + (int64_t)u * kThreads;
+    k[u] = kp[u] = kn[u] = kNoIndex;
+    if (i < a.n) {
+      k[u] = a.keyS[i];
+      kp[u] = i > 0 ? a.keyS[i - 1] : kNoIndex;
+      kn[u] = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;
+    }
+  }
+  const bool gather = !(a.merged && *a.merged);
+  const uint32_t ep = *a.epoch;
+#pragma unroll
+  for (int u = 0; u < kReorderSlots; ++u) {
+    const int64_t i = base + (int64_t)u * kThreads;
+    if (i < a.n) reorder_slot(a, i, k[u], kp[u], kn[u], gather, ep);
   }
 }
 
@@ -767,7 +789,7 @@ cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s) {
 
 cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
-  step_reorder<<<blocks_for(a.n, kThreads), kThreads, 0, s>>>(a);
+  step_reorder<<<blocks_for(a.n, kThreads * kReorderSlots), kThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
