@@ -325,12 +325,20 @@ static_assert(((1 << kGroupShift) % kThreads) == 0, "a force block lies inside o
 constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered together
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i);
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
 
 // Four blocks per SM (64 registers) for one instance, three for the batched
 // variants (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs a) {
+  // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
+  // recorded neighbours: one shared-memory load per pair instead of decoding k
+  __shared__ float2 unit[16];
+  if (threadIdx.x < 16) {
+    const int k = threadIdx.x;
+    unit[k] = k < 9 ? make_float2((float)(k / 3 - 1), (float)(k % 3 - 1)) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
   __shared__ uint32_t moved_in_block;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -338,7 +346,7 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs
   const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
   if (track && threadIdx.x == 0) moved_in_block = 0;
   uint32_t key = 0;
-  if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i);
+  if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, unit);
   if (track) {
     // slots whose cell key changed, for the incremental re-sort: one bit per
     // slot (a warp holds 32 consecutive slots), one count per block
@@ -356,7 +364,7 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs
 // Forces on particle i; in integrate mode also the update and the new key
 // (returned), in force-only mode the acceleration is stored.
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
+__device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit) {
   // one instance: a copy of the kernel-argument descriptor; batched: a reference
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
   const uint32_t key = a.keyA[i];
@@ -384,8 +392,9 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
       if (alpha_c0 > 0.f) {
         const float vr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy;
         if (vr < 0.f) {
-          // Monaghan: Pi_ij = -alpha c0 h vr / ((r^2 + eps h^2) rho_bar), rho_bar = (rho_i + rho_j) / 2
-          const float pij = -2.0f * alpha_c0 * h * vr * __fdividef(1.0f, (r2 + d.eps_h2) * (rho_i + 1.0f / vj.w));
+          // Monaghan: Pi_ij = -alpha c0 h vr / ((r^2 + eps h^2) rho_bar), rho_bar = (rho_i + rho_j) / 2,
+          // with rho_j = 1 / w_j: 1 / (rho_i + 1 / w_j) = w_j / (rho_i w_j + 1) -- one division
+          const float pij = -2.0f * alpha_c0 * h * vr * __fdividef(vj.w, (r2 + d.eps_h2) * fmaf(rho_i, vj.w, 1.0f));
           s = fmaf(d.ka, pij, s);
         }
       }
@@ -436,7 +445,13 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i) {
 #pragma unroll
       for (int u = 0; u < kForceBatch; ++u) {
         float dx, dy;
-        entry_vec<PREC>(d, pi, pj[u], e[u], dx, dy);
+        if (PREC == 1) {  // split: the offsets moved into one cell frame by the tag's stencil offset
+          const float2 o = unit[e[u] & 15u];
+          dx = (pi.x - pj[u].x) - o.x * d.cs_x;
+          dy = (pi.y - pj[u].y) - o.y * d.cs_y;
+        } else {
+          entry_vec<PREC>(d, pi, pj[u], e[u], dx, dy);
+        }
         pair_v(vj[u], dx, dy);
       }
     }
