@@ -68,8 +68,10 @@ cudaError_t launch_lists_count_scan(const StepArgs& a, int precision, int32_t* c
                                     int64_t* sums, cudaStream_t st);
 cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int64_t* offs,
                                      uint32_t* idx, int64_t cap, cudaStream_t st);
-// Per-instance diagnostics: partial sums per (chunk, instance) then a fixed-order
-// final sum; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx, sum m vy, nonfinite.
+// Per-instance diagnostics in one launch: float-float partials per (chunk,
+// instance) block, then the last block of an instance (ticket counter) sums them
+// in a fixed order; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx,
+// sum m vy, nonfinite.
 // Where the step headers of sphg_step_headers go: the caller's host array
 // (device-accessible), the index of the next step, and the count of instance
 // blocks done with the current one.
@@ -83,7 +85,7 @@ struct HeaderSlot {
 cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, uint32_t* tickets,
                                     int chunks, HeaderSlot* slot, cudaStream_t s);
 // The same into out[inst * 6 ..] (device-accessible).  partials: ninst x chunks
-// x 6 doubles; tickets: ninst counters, zero between launches.
+// 48-byte float-float records; tickets: ninst counters, zero between launches.
 cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, uint32_t* tickets, int chunks,
                                double* out, cudaStream_t s);
 // Diagnostics chunks of the largest instance (at most cap; the partial buffer
