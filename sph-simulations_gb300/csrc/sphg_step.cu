@@ -28,7 +28,7 @@
 
 namespace sphg {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;  // 128-thread blocks: measured a little faster than 256 and 512 for the passes
 
 // ---------------------------------------------------------------- keys
 template <int PREC, bool BATCHED>
@@ -327,10 +327,10 @@ constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered t
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
 
-// Four blocks per SM (64 registers) for one instance, three for the batched
-// variants (their instance lookup needs more registers).
+// Eight blocks per SM (64 registers) for one instance; the batched variants
+// are left to the compiler (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR>
-__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 4) step_force(StepArgs a) {
+__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 8) step_force(StepArgs a) {
   // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
   // recorded neighbours: one shared-memory load per pair instead of decoding k
   __shared__ float2 unit[16];
