@@ -53,6 +53,8 @@ def test_host_argument_checks_fail_before_any_device_work(built):
     assert L.sphg_step(None, 1, None) == S.INVALID_ARG
     assert L.sphg_preloop(None, None) == S.INVALID_ARG
     assert L.sphg_download(None, None, None, None, None, None, None, None, None, None) == S.INVALID_ARG
+    assert L.sphg_step_headers(None, 1, None, None) == S.INVALID_ARG
+    assert L.sphg_diagnostics_async(None, None, None) == S.INVALID_ARG
     # parameters the reference would accept silently and then misbehave on
     for bad in (dict(h=0.0), dict(h=-1.0), dict(dt=float("nan")), dict(hi=(0.0, 48.0)), dict(order=7)):
         p = S.params(**bad)
