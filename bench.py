@@ -357,7 +357,7 @@ def run_gpu(args):
                             if args.workload in TRAFFIC_PER_PARTICLE_STEP else None),
                 "traffic_unit": "DRAM bytes per main-loop iteration (ncu)",
                 "peak_source": src,
-                "kernel": "one main-loop iteration (radix sort + reorder + density + force)",
+                "kernel": "one main-loop iteration (re-sort or radix sort + reorder + density + force)",
                 "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP}
     names = ["keys", "sort", "reorder", "density", "force_integrate"]
     tot = sum(phase_ms)
