@@ -90,40 +90,14 @@ __device__ __forceinline__ void warp_count_below2(const unsigned long long* __re
   rb = lb + __popc(__ballot_sync(0xffffffffu, lessb));
 }
 
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* sh) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  uint32_t t = 0;
-  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
-  return t;
-}
-
+// One synchronisation for the whole block: the mover words are loaded first
+// (independent of the counts), then the totals over all groups and over the
+// groups before this one and the scan of the words' counts are reduced warp by
+// warp, and combined once.
 __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
-  __shared__ uint32_t red[kCompactThreads / 32];
-  __shared__ uint32_t scan[kCompactThreads / 32];
+  __shared__ uint32_t red_tot[kCompactThreads / 32], red_pre[kCompactThreads / 32], scan[kCompactThreads / 32];
   const int g = blockIdx.x;
   const int ngroups = (int)gridDim.x;
-  // movers in all groups, and in the groups before this one
-  uint32_t pre = 0, tot = 0;
-  for (int k = threadIdx.x; k < ngroups; k += blockDim.x) {
-    const uint32_t v = a.gsum[k];
-    tot += v;
-    if (k < g) pre += v;
-  }
-  tot = block_sum(tot, red);
-  pre = block_sum(pre, red);
-  const bool inc = tot <= (uint32_t)kMoverCap;
-  if (g == 0 && threadIdx.x == 0) {
-    a.ctl[0] = inc ? 1u : 0u;
-    a.ctl[1] = tot;
-    if (inc) *a.epoch += 1u;  // the step epoch the skipped radix sort would have bumped
-    if (a.cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, inc ? 0u : 1u);
-  }
-  if (!inc) return;
   const int64_t nwords = (a.n + 31) >> 5;
   const int64_t w0 = ((int64_t)g << (kGroupShift - 5)) + (int64_t)threadIdx.x * kCompactWords;
   uint32_t mw[kCompactWords];
@@ -133,18 +107,44 @@ __global__ void __launch_bounds__(kCompactThreads) movers_compact(MoverArgs a) {
     mw[q] = (w0 + q < nwords) ? a.mask[w0 + q] : 0u;
     c += __popc(mw[q]);
   }
-  // exclusive scan of the per-thread counts
+  // movers in all groups, and in the groups before this one
+  uint32_t pre = 0, tot = 0;
+  for (int k = threadIdx.x; k < ngroups; k += blockDim.x) {
+    const uint32_t v = a.gsum[k];
+    tot += v;
+    if (k < g) pre += v;
+  }
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  uint32_t x = c;
+  tot = __reduce_add_sync(0xffffffffu, tot);
+  pre = __reduce_add_sync(0xffffffffu, pre);
+  uint32_t x = c;  // inclusive scan of the per-thread counts within the warp
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
-  if (lane == 31) scan[wp] = x;
+  if (lane == 31) {
+    red_tot[wp] = tot;
+    red_pre[wp] = pre;
+    scan[wp] = x;
+  }
   __syncthreads();
+  tot = pre = 0;
   uint32_t wbase = 0;
-  for (int k = 0; k < wp; ++k) wbase += scan[k];
+#pragma unroll
+  for (int k = 0; k < kCompactThreads / 32; ++k) {
+    tot += red_tot[k];
+    pre += red_pre[k];
+    if (k < wp) wbase += scan[k];
+  }
+  const bool inc = tot <= (uint32_t)kMoverCap;
+  if (g == 0 && threadIdx.x == 0) {
+    a.ctl[0] = inc ? 1u : 0u;
+    a.ctl[1] = tot;
+    if (inc) *a.epoch += 1u;  // the step epoch the skipped radix sort would have bumped
+    if (a.cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, inc ? 0u : 1u);
+  }
+  if (!inc) return;
   uint32_t r = pre + wbase + x - c;
 #pragma unroll
   for (int q = 0; q < kCompactWords; ++q) {
