@@ -1,17 +1,22 @@
 // sphg_step.cu -- the per-step SPH kernels for sm_103a.
 //
-// Step pipeline (one launch each, plus the radix sort of sphg_sort.cu):
-//   step_keys      cell key of every particle of the next state
+// Step pipeline (one launch each, plus the re-sort of sphg_movers.cu or the
+// radix sort of sphg_sort.cu):
+//   step_keys      cell key of every particle (first iteration after an upload;
+//                  afterwards the force pass computes the next keys)
 //                  (GenericNeighborSearch::SetParticleCellIds, GenericNeighborSearch.h:201-231)
-//   [radix sort]   stable sort of (key, slot)           (SortParticleIds, :69-76)
-//   step_reorder   gather of the state into key order + cell ranges
-//                  (SortContainer :111-191, SetCellRanges :93-108)
+//   [re-sort]      stable order of (key, slot): merge of the slots that changed
+//                  cell, or the full radix sort (SortParticleIds, :69-76)
+//   step_reorder   cell ranges (and, after a full sort, the gather of the state
+//                  into key order) (SortContainer :111-191, SetCellRanges :93-108)
 //   step_density   3x3-stencil density + EOS pressure, stores p/rho^2 and 1/rho
 //                  (ApproximateDensity GenericForceComputation.tpp:35-130,
 //                   CalculatePressure :23-32, cuInvertDensity)
 //   step_force     pressure + viscosity (+ artificial viscosity) + gravity,
 //                  fused with the next step's symplectic-Euler update and walls
 //                  (ComputeForces :134-253, Integrator.cpp:7-46)
+//   step_diag      step-header diagnostics, when asked for (StepHeader,
+//                  app/simulation_configuration.h:152-158)
 //
 // Neighbour decisions and cell keys are the reference's FP64 decisions made
 // exactly from FP32 state: the FP32 value decides unless it lies in a thin
@@ -501,17 +506,6 @@ struct FFSum {
     c = __fadd_rn(c, __fadd_rn(e, err));
   }
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-  // the sum over a warp, still in float-float (lane 0 holds it)
-  __device__ __forceinline__ void warp_reduce() {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
-      float t, e;
-      two_sum(s, s2, t, e);
-      s = t;
-      c = __fadd_rn(c, __fadd_rn(c2, e));
-    }
-  }
 };
 
 // Per (chunk, instance) block.  The conservation sums (kinetic energy,
