@@ -341,8 +341,11 @@ def run_gpu(args):
         assert np.isfinite(hdr).all() and (hdr[:, 2::6].sum(axis=1) == n).all()
         assert np.isfinite(out["x"]).all()
     e2e_s = float(np.median(walls))
-    state_h2d = 8 + 8 + (4 if prec == sphg.SPLIT else 0)      # pos (or offset), vel, split cell key
-    state_d2h = 8 + 16 + 4 + (4 if prec == sphg.SPLIT else 0)  # pos, (v, p, 1/rho), rho, split cell key
+    # bytes that cross between host and device per particle: the caller's FP64
+    # x, y, vx, vy in; FP64 x, y, vx, vy, rho and int32 ids out (whether staged
+    # or read and written by the device in place)
+    state_h2d = 4 * 8
+    state_d2h = 5 * 8 + 4
     e2e = {"value": n * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(n * state_h2d / args.steps),
            "d2h_bytes_per_step": int(6 * 8 * ninst + n * state_d2h / args.steps),
