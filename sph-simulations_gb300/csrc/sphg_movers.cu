@@ -34,7 +34,7 @@ constexpr int kCompactThreads = 256;
 constexpr int kCompactWords = 1;  // words per thread: 256 x 1 word = one group of 8,192 slots
 static_assert(kCompactThreads * kCompactWords * 32 == (1 << kGroupShift), "one block per group");
 constexpr int kRankThreads = 256;  // 8 movers per block
-constexpr int kStayThreads = 256;
+constexpr int kStayThreads = 128;
 constexpr int kMergeSlots = 4;  // slots per thread of movers_merge
 
 __device__ __forceinline__ uint32_t movers_before(const MoverArgs& a, int64_t p, uint32_t m) {
