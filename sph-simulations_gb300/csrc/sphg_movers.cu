@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kRankThreads) movers_rank_place(MoverArgs a) {
   }
 }
 
-// Each block places kMergeSlots x 256 consecutive slots, those that kept their
+// Each block places kMergeSlots x kStayThreads consecutive slots, those that kept their
 // key (the movers are placed already): a stayer's position is its rank among
 // stayers + the movers ordered before it.  The movers ordered before any slot
 // of the block lie between the counts of its first and last slot, found by
