@@ -47,8 +47,8 @@ UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
 # DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
 # summed over one merge-path iteration's kernels, caches flushed before each captured
-# launch): 105.0 MB per iteration of 1,000,000 particles
-TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 105.0}
+# launch): 104.9 MB per iteration of 1,000,000 particles
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 104.9}
 L2_FLUSH_BYTES = 256 << 20
 E2E_TRIALS = 3
 
