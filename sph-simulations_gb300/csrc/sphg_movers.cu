@@ -17,8 +17,9 @@
 //
 // Kernels: movers_compact (mover list in slot order, movers before each word,
 // decision), movers_rank_place (a warp per mover: its rank by counting the
-// smaller movers, its final position by a warp-wide search of the slots),
-// movers_merge (final position of every stayer).
+// smaller movers, the stayers before it from the current cell-range table --
+// or a warp-wide search of the keys when its new cell is empty), movers_merge
+// (final position of every stayer).
 #include <cstdint>
 
 #include <cuda_runtime.h>
