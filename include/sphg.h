@@ -290,7 +290,12 @@ int32_t sphg_launches_per_step(const sphg_sim* s);
 
 /* Stand-alone kernels on caller-owned DEVICE buffers. */
 /* Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the keys.
- * keys_out/vals_out must not alias the inputs.  Scratch is allocated by this call. */
+ * keys_out/vals_out must not alias the inputs; vals_in == NULL sorts the
+ * identity 0..n-1.  Buffers need only 4-byte alignment.  n <= 2^30 - 1
+ * (SPHG_CAPACITY otherwise).  Scratch is allocated by this call.  Every wait of
+ * the sort's look-back is bounded; a wait that gives up (none does on a working
+ * GPU: it only waits on tiles that started earlier) is not reported by this
+ * stand-alone call. */
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                             uint32_t* vals_out, int64_t n, int32_t bits, void* stream);
 /* Largest n sphg_sort_pairs_noalloc accepts, and the size of its fixed scratch. */
@@ -304,7 +309,9 @@ sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, ui
  * the process exits), so n must be <= SPHG_SORT_NOALLOC_MAX_PAIRS
  * (SPHG_CAPACITY otherwise).  It calls no cudaMalloc/cudaFree.  The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  The address is looked up
+ * again when the device's context changes (after cudaDeviceReset the next call
+ * is a first call again).  All calls share the one
  * array: calls that overlap on the GPU (different streams, or different host
  * threads on one device) race and corrupt each other's results. */
 sphg_status sphg_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in,

@@ -17,7 +17,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsphref.so")
-REF_SRC = "/root/reference"
+# The reference checkout: SPH_REFERENCE_SRC, else a checkout named "reference"
+# beside this repository.
+REF_SRC = os.environ.get("SPH_REFERENCE_SRC") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)

@@ -485,8 +485,8 @@ sphg_status compute_layout(sphg_sim* s, int ninst, const sphg_params* p, const i
     L.n += counts[i];
     L.keys += (span + key_align - 1) / key_align * key_align;
     L.max_n = std::max(L.max_n, counts[i]);
-    if (L.n >= (int64_t)0x7fffffff || L.keys >= (uint64_t)0xfffffff0u)
-      return fail(SPHG_CAPACITY, "more than 2^31 particles or 2^32 cell keys in one handle");
+    if (L.n > sphg::kSortMaxKeys || L.keys >= (uint64_t)0xfffffff0u)
+      return fail(SPHG_CAPACITY, "more than 2^30-1 particles or 2^32 cell keys in one handle");
   }
   if (keys_cap && L.keys > keys_cap) return fail(SPHG_CAPACITY, "cell keys exceed the handle's key capacity");
   return SPHG_OK;
@@ -1227,7 +1227,7 @@ sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, ui
   if (n < 0 || bits < 1 || bits > 32) return fail(SPHG_INVALID_ARG, "n < 0 or bits outside 1..32");
   if (n == 0) return SPHG_OK;
   if (!keys_in || !keys_out || !vals_out) return fail(SPHG_INVALID_ARG, "null buffer");
-  if (n > 0x7fffffffLL) return fail(SPHG_CAPACITY, "n above 2^31-1");
+  if (n > sphg::kSortMaxKeys) return fail(SPHG_CAPACITY, "n above 2^30-1 (the sort's look-back counts)");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t words = sphg::sort_scratch_words(n) + ((bits > 8) ? 2 * (size_t)n : 0);
   uint32_t* scratch = nullptr;
@@ -1236,7 +1236,7 @@ sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, ui
   uint32_t* vtmp = ktmp + n;
   cudaError_t e = sphg::radix_sort_pairs(keys_in, vals_in, keys_out, vals_out,
                                          bits > 8 ? ktmp : nullptr, bits > 8 ? vtmp : nullptr,
-                                         scratch, n, bits, st);
+                                         scratch, n, bits, st, nullptr, nullptr, nullptr, true);
   cudaError_t e2 = cudaFreeAsync(scratch, st);
   SPHG_CUDA(e);
   SPHG_CUDA(e2);

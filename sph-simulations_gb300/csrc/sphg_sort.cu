@@ -62,7 +62,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_hist_all(const uint32_t* __
   for (int64_t b = (int64_t)blockIdx.x * chunk; b < n; b += (int64_t)gridDim.x * chunk) {
     const int64_t s0 = b + (int64_t)threadIdx.x * kHistPerThread;
     uint32_t k[kHistPerThread];
-    if (s0 + kHistPerThread <= n && ((s0 & 3) == 0)) {
+    // 16-byte loads only where the address allows them: a caller's buffer may
+    // start at any 4-byte boundary (a view such as keys + 1)
+    if (s0 + kHistPerThread <= n && ((reinterpret_cast<uintptr_t>(keys + s0) & 15u) == 0)) {
 #pragma unroll
       for (int q = 0; q < kHistPerThread; q += 4) {
         const uint4 v = __ldg(reinterpret_cast<const uint4*>(keys + s0 + q));
@@ -226,7 +228,7 @@ cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
                              cudaStream_t stream, uint32_t* epoch, const uint32_t* hist,
-                             const uint32_t* skip) {
+                             const uint32_t* skip, bool clear_err) {
   if (n <= 0) return cudaSuccess;
   const int passes = passes_for(bits);
   // big inputs: 4096-key tiles halve the look-back chain; small ones: 2048 for parallelism
@@ -237,13 +239,15 @@ cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
   uint32_t* err = tile_counter + kMaxPasses;
   uint32_t* lookback = scratch + head_words();
   // tile counters and look-back words start at zero every sort; so does the
-  // histogram unless the caller accumulated it already (the error word is left
-  // alone: it stays set until the caller clears it)
+  // histogram unless the caller accumulated it already.  The error word is
+  // cleared too when clear_err is set (stand-alone sorts); a step's sort leaves
+  // it alone so it stays set until the handle reports it.
   cudaError_t e;
+  const size_t head_clear = kMaxPasses + (clear_err ? 1 : 0);
   if (hist) {
-    e = cudaMemsetAsync(tile_counter, 0, sizeof(uint32_t) * kMaxPasses, stream);
+    e = cudaMemsetAsync(tile_counter, 0, sizeof(uint32_t) * head_clear, stream);
   } else {
-    e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + kMaxPasses), stream);
+    e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + head_clear), stream);
   }
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * (size_t)passes * kRadix * ntiles, stream);

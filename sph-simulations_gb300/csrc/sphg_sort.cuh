@@ -24,11 +24,17 @@ uint32_t* sort_error_word(uint32_t* scratch);
 // d of pass p at p*256 + d, summed over all keys); otherwise they are computed.
 // When *skip (device word, read by the kernels) is non-zero the kernels return
 // at once: the step's incremental re-sort produced the result instead.
+// clear_err: zero the error word first (stand-alone sorts, whose callers have
+// no handle that reports it).  n must not exceed kSortMaxKeys.
 cudaError_t radix_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                              uint32_t* keys_out, uint32_t* vals_out, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* scratch, int64_t n, int bits,
                              cudaStream_t stream, uint32_t* epoch = nullptr,
-                             const uint32_t* hist = nullptr, const uint32_t* skip = nullptr);
+                             const uint32_t* hist = nullptr, const uint32_t* skip = nullptr,
+                             bool clear_err = false);
+// Largest n the sort accepts: a look-back word keeps a running count in 30 bits
+// under its two flag bits.
+constexpr int64_t kSortMaxKeys = ((int64_t)1 << 30) - 1;
 constexpr int kSortMaxPasses = 4;
 
 }  // namespace sphg

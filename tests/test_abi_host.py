@@ -65,6 +65,11 @@ def test_host_argument_checks_fail_before_any_device_work(built):
     assert L.sphg_create(ctypes.byref(p), ctypes.byref(o), 10, ctypes.byref(h)) == S.INVALID_ARG
     o = S.options(tile_bits=4)  # tiles need Morton order; the default params are rowmajor
     assert L.sphg_create(ctypes.byref(p), ctypes.byref(o), 10, ctypes.byref(h)) == S.INVALID_ARG
+    # the sorts keep 30-bit running counts in their look-back words
+    sort = L.sphg_sort_pairs
+    sort.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]
+    assert sort(16, 16, 32, 32, 1 << 30, 22, None) == S.CAPACITY
+    assert "2^30" in L.sphg_last_error_string().decode()
 
 
 def _write_cfg(path, **kv):

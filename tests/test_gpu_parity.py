@@ -103,6 +103,28 @@ def test_sort_pairs_stable(n, bits):
     assert (vo.cpu().numpy().view(np.uint32) == vals[order]).all()
 
 
+@pytest.mark.parametrize("offset", [1, 2, 3])
+def test_sort_pairs_from_unaligned_views(offset):
+    """Caller buffers that start at any 4-byte boundary (keys[offset:]): the
+    histogram pass takes 16-byte loads only where the address allows them."""
+    torch = pytest.importorskip("torch")
+    S = _sphg()
+    n = 100003
+    rng = np.random.default_rng(offset)
+    keys = rng.integers(0, 1 << 20, n + offset, dtype=np.uint64).astype(np.uint32)
+    keys[offset: offset + n // 4] = 7  # runs of equal keys
+    base = torch.from_numpy(keys.view(np.int32)).cuda()
+    ki = base[offset:]
+    assert ki.data_ptr() % 16 != 0
+    ko = torch.empty(n, dtype=torch.int32, device="cuda")
+    vo = torch.empty(n, dtype=torch.int32, device="cuda")
+    S.sort_pairs(ki.data_ptr(), 0, ko.data_ptr(), vo.data_ptr(), n, 20)
+    torch.cuda.synchronize()
+    order = np.argsort(keys[offset:], kind="stable")
+    assert (ko.cpu().numpy().view(np.uint32) == keys[offset:][order]).all()
+    assert (vo.cpu().numpy() == order).all()
+
+
 # ---------------------------------------------------------------- whole step vs reference goldens
 def test_preloop_matches_reference_dam12k(golden):
     """12,800-particle dam-break geometry, reference physics (k=30, rho0=25, mu=0.01,
