@@ -239,12 +239,19 @@ sphg_status sphg_restore(sphg_sim* s, const void* buf, uint64_t bytes, void* str
 /* ---- continuous batching ("serving").  A server owns one device arena sized
  * from an HBM budget and keeps every live simulation's state resident in it.
  * Submitted requests queue in order; every tick admits the queue head while
- * the live set fits the budget, runs one batched main-loop iteration of all
- * live simulations (a newcomer's first iteration is its pre-loop), and retires
- * the ones that ran `steps` iterations (the reference's `steps` key: the
- * pre-loop plus steps-1 main-loop iterations).  A simulation gives the same
- * bits whatever else is live.  No reference counterpart: the reference runs
- * one simulation per process (app/main.cpp:20-56). */
+ * it fits (appended after the slots in use, so running simulations keep their
+ * slots; the live set is compacted when the arena's end is reached or
+ * finished simulations hold more slots than live ones), runs one batched
+ * main-loop iteration of all live simulations from a CUDA graph (a newcomer's
+ * first iteration is its pre-loop), and retires the ones that ran `steps`
+ * iterations (the reference's `steps` key: the pre-loop plus steps-1 main-loop
+ * iterations) by an asynchronous copy into pinned host memory.  A simulation
+ * gives the same bits whatever else is live.  The serving loop runs either on
+ * the caller's thread (sphg_server_tick) or on a thread and stream of the
+ * server's own (sphg_server_start), which admits arrivals while earlier ticks
+ * run on the GPU.  submit, result and stats may be called from any thread.
+ * No reference counterpart: the reference runs one simulation per process
+ * (app/main.cpp:20-56). */
 typedef struct sphg_server sphg_server;
 sphg_status sphg_server_create(double hbm_budget_bytes, int32_t max_instances,
                                const sphg_options* o, sphg_server** out);
@@ -256,16 +263,30 @@ sphg_status sphg_server_submit(sphg_server* s, const sphg_params* p, int64_t n, 
  * lattice, nx * ny particles): no host arrays cross the boundary for it. */
 sphg_status sphg_server_submit_lattice(sphg_server* s, const sphg_params* p, const sphg_lattice* spec,
                                        int64_t steps, int64_t* request_id);
-/* Admit, step, retire.  *live = simulations live after the tick, *finished = retired by it. */
+/* Admit, step, retire on the caller's thread and stream.  *live = simulations
+ * live after the tick, *finished = retired by it.  SPHG_INVALID_ARG while the
+ * serving thread runs. */
 sphg_status sphg_server_tick(sphg_server* s, void* stream, int32_t* live, int32_t* finished);
+/* Starts the serving thread on `device` with a stream of its own: it ticks
+ * while anything is live or queued (at most three ticks ahead of the GPU) and
+ * waits for submissions otherwise. */
+sphg_status sphg_server_start(sphg_server* s, int32_t device);
+/* Stops and joins the serving thread (live and queued requests stay; ticks can
+ * continue with sphg_server_tick).  Reports an error the thread stopped on. */
+sphg_status sphg_server_stop(sphg_server* s);
 /* Final state of a finished request (slot order, like sphg_download) and its
- * latency (completion - submission, seconds); SPHG_NOT_READY until then.  The
- * result is released once fetched. */
+ * latency (time its result reached host memory - submission, seconds);
+ * SPHG_NOT_READY until then (without the serving thread, a request retired by
+ * the last tick waits for its copy here).  The result is released once fetched. */
 sphg_status sphg_server_result(sphg_server* s, int64_t request_id, double* x, double* y, double* vx,
                                double* vy, double* rho, int32_t* ids, double* latency_s);
 /* out[8]: live, queued, completed, particle-steps run, ticks, capacity (particles),
  * capacity (cell keys), live particles. */
 sphg_status sphg_server_stats(sphg_server* s, double* out);
+/* The first `count` of: appends, compactions, graph builds, slots of finished
+ * simulations awaiting compaction, slots in use, result copies in flight,
+ * serving thread running (1/0). */
+sphg_status sphg_server_counters(sphg_server* s, double* out, int32_t count);
 
 /* Autotuner: times every candidate launch configuration of this workload (the
  * cell-block shape: one thread per particle or Morton cell tiles of 2^b x 2^b

@@ -105,6 +105,7 @@ sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64
   d.nyr = nr[1];
   d.order = p.order;
   d.periodic = p.periodic ? 1 : 0;
+  d.active = 1;
   if (p.order == SPHG_ORDER_MORTON) {
     d.nx = next_pow2(nr[0]);
     d.ny = next_pow2(nr[1]);
@@ -401,7 +402,7 @@ sphg_status build_graph_conditional(sphg_sim* s, cudaGraphExec_t* exec, bool hea
 
 // The graph of one iteration (header: followed by its step header into the
 // header slot).
-sphg_status build_graph(sphg_sim* s, bool header = false) {
+sphg_status build_graph(sphg_sim* s, bool header) {
   cudaGraphExec_t* exec = header ? &s->gexec_hdr : &s->gexec;
   if (*exec) return SPHG_OK;
   if (!s->cap_stream) SPHG_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));

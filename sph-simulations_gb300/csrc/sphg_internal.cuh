@@ -177,6 +177,9 @@ uint32_t morton_host(uint32_t x, uint32_t y);
 void demorton_host(uint32_t z, int& x, int& y);
 // One main-loop iteration on st; ev (6 events, optional) records the phase boundaries.
 sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false, cudaEvent_t* ev = nullptr);
+// Captures (once per layout) the CUDA graph of one iteration (header: followed
+// by its step header into the header slot).
+sphg_status build_graph(sphg_sim* s, bool header = false);
 
 struct Layout {
   std::vector<InstDesc> desc;

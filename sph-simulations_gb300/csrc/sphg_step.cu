@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
+  if (BATCHED && !d.active) return;  // a finished served instance
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   typename std::conditional<PREC == 1, CSum, PSum>::type S;
@@ -347,7 +348,8 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 8) step_force(StepArgs
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
   __shared__ uint32_t moved_in_block;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < a.n;
+  // slots of a finished served instance are skipped (no pair, no integration, no mover bit)
+  const bool valid = i < a.n && (!BATCHED || inst_ref<BATCHED>(a, i).active);
   const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
   if (track && threadIdx.x == 0) moved_in_block = 0;
   uint32_t key = 0;
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 8) step_force(StepArgs
     // slots whose cell key changed, for the incremental re-sort: one bit per
     // slot (a warp holds 32 consecutive slots), one count per block
     const unsigned moved = __ballot_sync(0xffffffffu, valid && key != a.keyA[i]);
-    if ((threadIdx.x & 31) == 0 && valid) {
+    if ((threadIdx.x & 31) == 0 && i < a.n) {  // every word of the slots, skipped ones included
       a.mover_mask[i >> 5] = moved;
       if (moved) atomicAdd(&moved_in_block, (uint32_t)__popc(moved));
     }

@@ -105,8 +105,12 @@ def lib():
         L.sphg_server_tick.argtypes = [SP, _vp, _ip, _ip]
         L.sphg_server_result.argtypes = [SP, ctypes.c_int64] + [_dp] * 5 + [_ip, _dp]
         L.sphg_server_stats.argtypes = [SP, _dp]
+        L.sphg_server_start.argtypes = [SP, ctypes.c_int32]
+        L.sphg_server_stop.argtypes = [SP]
+        L.sphg_server_counters.argtypes = [SP, _dp, ctypes.c_int32]
         for f in ("sphg_server_create", "sphg_server_destroy", "sphg_server_submit",
-                  "sphg_server_tick", "sphg_server_result", "sphg_server_stats"):
+                  "sphg_server_tick", "sphg_server_result", "sphg_server_stats", "sphg_server_start",
+                  "sphg_server_stop", "sphg_server_counters"):
             getattr(L, f).restype = ctypes.c_int
         L.sphg_sort_pairs.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp]
         L.sphg_cell_keys.argtypes = [PP, _vp, _vp, ctypes.c_int64, _vp, _vp]
@@ -420,7 +424,19 @@ class Server:
         check(lib().sphg_server_stats(self._h, _ptr(out)))
         keys = ("live", "queued", "completed", "particle_steps", "ticks", "cap_particles",
                 "cap_keys", "live_particles")
-        return dict(zip(keys, out.tolist()))
+        d = dict(zip(keys, out.tolist()))
+        c = np.zeros(7, np.float64)
+        check(lib().sphg_server_counters(self._h, _ptr(c), 7))
+        d.update(zip(("appends", "compactions", "graph_builds", "finished_slots", "slots_in_use",
+                      "copies_in_flight", "thread_running"), c.tolist()))
+        return d
+
+    def start(self, device=0):
+        """Serving thread with its own stream: ticks while work is live or queued."""
+        check(lib().sphg_server_start(self._h, int(device)))
+
+    def stop(self):
+        check(lib().sphg_server_stop(self._h))
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

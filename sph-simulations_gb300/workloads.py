@@ -14,6 +14,10 @@ are the library's extensions.
                           (256 boxes of 2,000-65,536 particles)
   requests(rate, seconds) a Poisson stream of dam-break / Taylor-Green jobs
                           (200 per second, 1,000-200,000 particles)
+  lattice_requests(...)   the same stream as lattice specifications whose
+                          initial states the device generates at admission
+                          (no host particle arrays: a 60 s window holds
+                          12,000 requests, ~450M particles)
 """
 import math
 
@@ -153,4 +157,47 @@ def requests(rate=200.0, seconds=60.0, seed=0, nmin=1000, nmax=200000, steps=500
             n = max(8, int(round(math.sqrt(npart))))
             prm, x, y, vx, vy, _ = taylor_green(n, seed=int(rng.integers(1 << 30)))
             out.append((t, "tgv", prm, x, y, vx, vy, steps))
+    return out
+
+
+def lattice_requests(rate=200.0, seconds=60.0, seed=0, nmin=1000, nmax=200000, steps=500):
+    """Poisson arrivals as lattice specifications: list of (arrival_time_s, kind,
+    params, spec, steps, particles); spec holds the keyword arguments of
+    sphg.lattice (x0, y0, dx, dy, nx, ny, jitter, seed, velocity, u0).  kind is
+    'dam' (a jittered column at rest, dam_break_sized's geometry) or 'tgv' (the
+    periodic Taylor-Green vortex, taylor_green's parameters), 50/50; particle
+    counts log-uniform in [nmin, nmax]."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        npart = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        jseed = int(rng.integers(1 << 62))
+        if rng.uniform() < 0.5:
+            aspect = rng.uniform(0.3, 2.0)
+            dx = 0.005
+            nx = max(2, int(round(math.sqrt(npart / aspect))))
+            ny = max(2, int(round(npart / nx)))
+            h = 1.3 * dx
+            prm = dict(order="morton", h=h, dt=1e-5, k=K_STIFF, rho0=RHO0, mu=0.0, gx=0.0, gy=-9.81,
+                       mass=lattice_mass(RHO0, h, dx), alpha=0.1, c0=math.sqrt(K_STIFF),
+                       lo=(0.0, 0.0), hi=(2.5 * nx * dx, 1.25 * ny * dx), periodic=0)
+            spec = dict(x0=0.5 * dx, y0=0.5 * dx, dx=dx, dy=dx, nx=nx, ny=ny, jitter=0.01, seed=jseed,
+                        velocity=0, u0=0.0)
+            out.append((t, "dam", prm, spec, steps, nx * ny))
+        else:
+            n = max(8, int(round(math.sqrt(npart))))
+            dx = 1.0 / n
+            h = 1.3 * dx
+            mass = lattice_mass(RHO0, h, dx)
+            kappa = laplacian_lattice_factor(h, dx, mass, RHO0)
+            prm = dict(order="morton", h=h, dt=2e-5, k=K_STIFF, rho0=RHO0, mu=0.01 / kappa, gx=0.0, gy=0.0,
+                       mass=mass, alpha=0.0, c0=math.sqrt(K_STIFF), lo=(0.0, 0.0), hi=(1.0, 1.0),
+                       periodic=1)
+            spec = dict(x0=0.5 * dx, y0=0.5 * dx, dx=dx, dy=dx, nx=n, ny=n, jitter=0.01, seed=jseed,
+                        velocity=1, u0=1.0)
+            out.append((t, "tgv", prm, spec, steps, n * n))
     return out

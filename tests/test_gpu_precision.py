@@ -7,6 +7,14 @@ precision modes:
   * positions, free-running: the GPU run against the oracle run from the same
     initial state, particles matched by creation index, max |dx| in units of
     the lattice spacing.
+Cell keys and neighbour sets are checked independently of the GPU:
+  * the oracle's own cell keys of the downloaded FP64 positions must equal the
+    GPU's keys, except where the test shows the position lies within 1e-9 of a
+    cell edge (in split precision the FP64 reconstruction lo + c cs + o of an
+    offset just inside its cell can round onto the edge); those are counted;
+  * the neighbour lists of the whole 1,000,000-particle state
+    (sphg_neighbor_lists) must equal the oracle's lists
+    (MultipassNeighborLists order, self included) bit for bit.
 The figures are printed as one PRECISION_REPORT line (pytest -s)."""
 import json
 
@@ -19,6 +27,26 @@ pytestmark = pytest.mark.gpu
 
 RHO_TOL = 1e-5
 ACC_TOL = 1e-5
+
+
+def _edge_distance(prm, x, y):
+    """Distance of each position to the nearest cell edge, in cells."""
+    cs = prm["h"]
+    fx = (np.asarray(x) - prm["lo"][0]) / cs
+    fy = (np.asarray(y) - prm["lo"][1]) / cs
+    return np.minimum(np.abs(fx - np.round(fx)), np.abs(fy - np.round(fy)))
+
+
+def independent_keys(prm, p, g, keys):
+    """The oracle's keys of the downloaded positions against the GPU's keys:
+    every difference must sit within 1e-9 of a cell edge.  Returns the number
+    of such differences."""
+    own = O.cell_ids(p, g["x"], g["y"])
+    off = np.nonzero(own != keys)[0]
+    if len(off):
+        d = _edge_distance(prm, g["x"][off], g["y"][off])
+        assert np.all(d < 1e-9), (len(off), off[np.argmax(d)], float(d.max()))
+    return int(len(off))
 
 
 def _errors(p, g, keys):
@@ -59,21 +87,22 @@ def test_precision_report_1m_dam_break():
             sim.step(k - done)
             g = sim.download()
             keys = sim.debug(S.DBG_KEYS)
-            recomputed = O.cell_ids(p, g["x"], g["y"])
-            off = np.nonzero(recomputed != keys)[0]
+            at_edge = independent_keys(prm, p, g, keys)
             if mode == "plain":
-                assert len(off) == 0
-            else:  # only reconstructions that land within rounding of a cell edge
-                cs = prm["h"]
-                for q in off[:50]:
-                    fx_ = (g["x"][q] - prm["lo"][0]) / cs
-                    fy_ = (g["y"][q] - prm["lo"][1]) / cs
-                    edge = min(abs(fx_ - round(fx_)), abs(fy_ - round(fy_)))
-                    assert edge < 1e-9, (mode, k, q, g["x"][q], g["y"][q])
+                assert at_edge == 0  # FP32 positions: the oracle's keys of the same values
+            # neighbour sets of the whole state, bit for bit: the oracle walks the
+            # cells of the GPU's keys (its own keys wherever they are defined apart
+            # from the edge cases counted above)
+            s_, e_ = O.cell_ranges(p, keys)
+            ro, ri = O.neighbor_lists(p, g["x"], g["y"], keys, s_, e_)
+            go, gi = sim.neighbor_lists()
+            assert np.array_equal(go, ro), (mode, k, "list offsets")
+            assert np.array_equal(gi, ri), (mode, k, "list entries")
             drho, dacc = _errors(p, g, keys)
             dpos = float(np.max(np.hypot(g["x"] - rpos[g["ids"], 0], g["y"] - rpos[g["ids"], 1])) / dx)
             report["%s_step%d" % (mode, k)] = {"density_rel": drho, "accel_rel": dacc, "pos_over_dx": dpos,
-                                               "cells_at_rounding_edge": int(len(off))}
+                                               "cells_at_rounding_edge": at_edge,
+                                               "neighbour_entries_exact": int(len(gi))}
         done = k
     for sim in sims.values():
         sim.close()

@@ -146,3 +146,73 @@ def test_lattice_requests_equal_host_array_requests(prec):
             assert (a[f] == b[f]).all(), f
         else:
             np.testing.assert_allclose(a[f], b[f], rtol=1e-6, atol=1e-7 * np.abs(b[f]).max())
+
+
+def _alone_map(S, reqs):
+    return [_serve(S, [r])[0][0] for r in reqs]
+
+
+def test_serving_thread_overlaps_arrivals_and_matches_alone():
+    """The serving thread (own thread and stream) admits requests that arrive
+    while others run; every result equals the same request served alone, bit
+    for bit, and newcomers were appended without moving the running ones."""
+    import time
+
+    import sphg as S
+    reqs = _requests(4, 12)
+    srv = S.Server(2e9)
+    srv.start()
+    ids = []
+    for k, (prm, x, y, vx, vy, steps) in enumerate(reqs):
+        ids.append(srv.submit(S.params(**prm), x, y, vx, vy, steps))
+        time.sleep(0.002 * (k % 3))
+    results = {}
+    t0 = time.time()
+    while len(results) < len(ids) and time.time() - t0 < 60:
+        for rid in ids:
+            if rid not in results:
+                r = srv.result(rid)
+                if r is not None:
+                    results[rid] = r
+        time.sleep(0.001)
+    st = srv.stats()
+    srv.stop()
+    srv.close()
+    assert len(results) == len(ids)
+    assert st["thread_running"] == 1 and st["appends"] >= 1
+    alone = _alone_map(S, reqs)
+    for k, rid in enumerate(ids):
+        for f in ("x", "y", "vx", "vy", "rho", "ids"):
+            assert (results[rid][f] == alone[k][f]).all(), (k, f)
+        assert results[rid]["latency_s"] > 0
+
+
+def test_compaction_keeps_every_result_bitwise():
+    """A budget small enough that finished requests' slots must be reclaimed:
+    the live set is compacted (dense repack + full sort) and every result still
+    equals the request served alone."""
+    import sphg as S
+    reqs = _requests(5, 14)
+    budget = 2 * 160.0 * 9000
+    srv = S.Server(budget)
+    cap = srv.stats()["cap_particles"]
+    reqs = [r for r in reqs if len(r[1]) <= cap]
+    ids = [srv.submit(S.params(**r[0]), *r[1:5], r[5]) for r in reqs]
+    done = {}
+    for _ in range(20000):
+        srv.tick()
+        for rid in ids:
+            if rid not in done:
+                r = srv.result(rid)
+                if r is not None:
+                    done[rid] = r
+        if len(done) == len(ids):
+            break
+    st = srv.stats()
+    srv.close()
+    assert len(done) == len(ids)
+    assert st["compactions"] >= 1 and st["appends"] >= 1
+    alone = _alone_map(S, reqs)
+    for k, rid in enumerate(ids):
+        for f in ("x", "y", "vx", "vy", "rho", "ids"):
+            assert (done[rid][f] == alone[k][f]).all(), (k, f)
