@@ -492,10 +492,10 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     name = args.workload
     prec = sphg.SPLIT if WORKLOADS[name]["precision"] == "split" else sphg.PLAIN
-    opts = sphg.options(precision=prec, track_ids=0, use_graph=1)
+    opts = sphg.options(precision=prec, track_ids=0, use_graph=args.graph)
     is_batch = WORKLOADS[name]["kind"] == "batch"
     rec, (w, prm, x, y, vx, vy) = device_record(name, args, opts, stream, args.steps, args.warmup,
-                                                world=world, tune=is_batch)
+                                                world=world, tune=is_batch and args.graph == 1)
     extra = {}
     if is_batch:
         tuned_opts = opts
@@ -566,6 +566,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of CPU baseline sampling (0 = skip)")
+    ap.add_argument("--graph", type=int, default=1,
+                    help="1: every iteration replays a CUDA graph; 0: stream-launched kernels (for profilers)")
     ap.add_argument("--no-nested", action="store_true",
                     help="only the named workload (no nested dam_break_1m / serve records)")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")

@@ -229,12 +229,9 @@ sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond
   sphg::MoverArgs m;
   m.n = s->n;
   m.keyA = s->keyA;
-  m.keyB = s->keyB;
   m.mask = s->mmask;
-  m.gsum = s->mgsum;
-  m.wprefix = s->mwprefix;
   m.movers = s->mlist;
-  m.msorted = s->msorted;
+  m.count = s->flags + 7;
   m.ctl = s->flags + 3;
   m.epoch = s->flags + 2;
   m.ranges = s->ranges;
@@ -264,8 +261,8 @@ sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
-  // group counts of this iteration's force pass (the re-sort has read the last ones)
-  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->mgsum, 0, sizeof(uint32_t) * s->mgroups, st));
+  // the mover count of this iteration's force pass (the re-sort has read the last one)
+  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->flags + 7, 0, sizeof(uint32_t), st));
   SPHG_CUDA(sphg::launch_reorder(a, st));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[3], st));
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
@@ -532,12 +529,8 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
       s->ncount = A.take<uint32_t>(N);
     }
     if (s->movers_on) {
-      s->mgroups = sphg::mover_groups((int64_t)N);
       s->mmask = A.take<uint32_t>((N + 31) / 32);
-      s->mwprefix = A.take<uint32_t>((N + 31) / 32);
-      s->mgsum = A.take<uint32_t>(s->mgroups);
       s->mlist = A.take<unsigned long long>(sphg::kMoverCap);
-      s->msorted = A.take<unsigned long long>(sphg::kMoverCap);
     }
     if (s->opt.compute == SPHG_COMPUTE_LISTS) {
       s->csr_counts = A.take<int32_t>(N);
@@ -1220,7 +1213,7 @@ int32_t sphg_launches_per_step(const sphg_sim* s) {
   // reorder + density + force (+ the three incremental re-sort kernels; + list
   // count, three scan kernels and list fill in the lists mode).  An iteration
   // that merges launches (key_bits + 7) / 8 + 1 kernels fewer in a graph.
-  return passes + 4 + (s->movers_on ? 3 : 0) + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
+  return passes + 4 + (s->movers_on ? 1 : 0) + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
 }
 
 sphg_status sphg_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

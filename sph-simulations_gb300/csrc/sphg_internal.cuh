@@ -71,9 +71,8 @@ struct sphg_sim {
   // incremental re-sort: mover bits and group counts written by the force pass
   bool movers_on = false;
   bool force_full_sort = false;  // the next iteration sorts fully (the slot record is stale)
-  uint32_t *mmask = nullptr, *mgsum = nullptr, *mwprefix = nullptr;
-  unsigned long long *mlist = nullptr, *msorted = nullptr;
-  int mgroups = 0;
+  uint32_t* mmask = nullptr;
+  unsigned long long* mlist = nullptr;
   size_t cap_n = 0;             // arena capacity (particles)
   uint64_t cap_keys = 0;        // arena capacity (cell keys)
   int cap_inst = 0;             // arena capacity (instances)
@@ -137,7 +136,8 @@ struct sphg_sim {
     a.keyS = keyTmp;
     a.merged = movers_on ? flags + 3 : nullptr;
     a.mover_mask = movers_on ? mmask : nullptr;
-    a.mover_gsum = movers_on ? mgsum : nullptr;
+    a.mover_list = movers_on ? mlist : nullptr;
+    a.mover_count = movers_on ? flags + 7 : nullptr;
     return a;
   }
 };

@@ -5,21 +5,17 @@
 
 namespace sphg {
 
-constexpr int kGroupShift = 13;   // slots per mover group count: 8,192
 constexpr int kMoverCap = 8192;   // largest mover set merged incrementally
 
 struct MoverArgs {
   int64_t n;
   const uint32_t* keyA;    // sorted keys of the current state, slot order
-  const uint32_t* keyB;    // keys of the integrated state, per slot
   const uint32_t* mask;    // [ceil(n/32)] bit s%32 of word s/32: slot s changed key
-  const uint32_t* gsum;    // [mover_groups(n)] changed slots per group of 8,192 slots
-  uint32_t* wprefix;       // [ceil(n/32)] changed slots before each word
-  unsigned long long* movers;   // [kMoverCap] key << 32 | slot, slot order
-  unsigned long long* msorted;  // [kMoverCap] the same, ascending
+  const unsigned long long* movers;  // [kMoverCap] key << 32 | slot of every changed slot, any order
+  const uint32_t* count;   // changed slots the force pass recorded (may exceed kMoverCap)
   uint32_t* ctl;           // [0] = 1 when the incremental path ran, [1] = changed slots,
                            // [2] set to 1 if a record was inconsistent (never cleared here)
-  uint32_t* epoch;         // step epoch of the cell-range table
+  uint32_t* epoch;         // step epoch of the cell-range table (bumped when the merge runs)
   const uint4* ranges;     // cell ranges {start, end, epoch, 0} of the current sorted order
   uint32_t* keyS;          // out: sorted keys
   uint32_t* perm;          // out: previous slot of each sorted position
@@ -35,9 +31,9 @@ struct MoverArgs {
   int32_t* idsA;
 };
 
-int mover_groups(int64_t n);
-// movers_compact, movers_rank_place, movers_merge; when more than kMoverCap
-// slots changed they do nothing and leave ctl[0] = 0 for the full sort.
+// One launch: the decision (merge when at most kMoverCap slots changed, else
+// leave ctl[0] = 0 for the full sort), the final position of every unchanged
+// slot and of every changed one, and the scatter of the state.
 cudaError_t launch_movers(const MoverArgs& a, cudaStream_t st);
 
 }  // namespace sphg

@@ -551,9 +551,11 @@ sphg_status tick_impl(sphg_server* s, cudaStream_t st, int32_t* live_out, int32_
       for (const SlotEntry& e : cand)
         if (e.live) dense.push_back(e);
       if (layout_of(s, dense, L) != SPHG_OK) break;  // does not fit even densely: wait
-      // staging of a compaction holds the current slots plus the newcomers
-      if ((size_t)(sim->n + add_n + r.n) > sim->cap_n) break;
       do_compact = true;
+      // staging of a compaction holds the current slots plus the newcomers: when
+      // they do not fit, this tick compacts what is admitted so far and the head
+      // follows once finished instances' slots are reclaimed
+      if ((size_t)(sim->n + add_n + r.n) > sim->cap_n) break;
     }
     admit.push_back(head);
     add_n += r.n;

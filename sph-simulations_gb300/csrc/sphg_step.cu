@@ -324,7 +324,6 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 // The pairs are the neighbours the density pass recorded (j << 5 | stencil
 // tag per entry); a particle with more than the recorded slots walks the
 // stencil again.
-static_assert(((1 << kGroupShift) % kThreads) == 0, "a force block lies inside one mover group");
 #ifndef SPHG_FORCE_BATCH
 #define SPHG_FORCE_BATCH 4
 #endif
@@ -346,25 +345,26 @@ __global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 8) step_force(StepArgs
   }
   __syncthreads();
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
-  __shared__ uint32_t moved_in_block;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // slots of a finished served instance are skipped (no pair, no integration, no mover bit)
   const bool valid = i < a.n && (!BATCHED || inst_ref<BATCHED>(a, i).active);
   const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
-  if (track && threadIdx.x == 0) moved_in_block = 0;
   uint32_t key = 0;
   if (valid) key = force_one<PREC, BATCHED, MODE, CSR>(a, i, unit);
   if (track) {
     // slots whose cell key changed, for the incremental re-sort: one bit per
-    // slot (a warp holds 32 consecutive slots), one count per block
+    // slot (a warp holds 32 consecutive slots) and (key, slot) appended to the
+    // mover list, one atomic per warp
     const unsigned moved = __ballot_sync(0xffffffffu, valid && key != a.keyA[i]);
-    if ((threadIdx.x & 31) == 0 && i < a.n) {  // every word of the slots, skipped ones included
-      a.mover_mask[i >> 5] = moved;
-      if (moved) atomicAdd(&moved_in_block, (uint32_t)__popc(moved));
+    const int lane = threadIdx.x & 31;
+    if (lane == 0 && i < a.n) a.mover_mask[i >> 5] = moved;  // every word of the slots, skipped ones included
+    if (moved) {
+      uint32_t at = 0;
+      if (lane == 0) at = atomicAdd(a.mover_count, (uint32_t)__popc(moved));
+      at = __shfl_sync(0xffffffffu, at, 0) + (uint32_t)__popc(moved & ((1u << lane) - 1u));
+      if (((moved >> lane) & 1u) && at < (uint32_t)kMoverCap)
+        a.mover_list[at] = ((unsigned long long)key << 32) | (uint32_t)i;
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && moved_in_block)
-      atomicAdd(a.mover_gsum + (((int64_t)blockIdx.x * blockDim.x) >> kGroupShift), moved_in_block);
   }
 }
 

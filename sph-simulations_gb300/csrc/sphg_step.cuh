@@ -44,7 +44,8 @@ struct StepArgs {
   const uint32_t* csr_idx;     // j << 5 | tag entries, self included, list order
   const uint32_t* merged;      // non-null and set: this iteration's merge scattered the state (reorder: ranges only)
   uint32_t* mover_mask;        // [ceil(n/32)] force pass: bit per slot whose key changed (or null)
-  uint32_t* mover_gsum;        // [groups of 65,536 slots] changed slots per group (zeroed before)
+  unsigned long long* mover_list;  // [kMoverCap] force pass: key << 32 | slot of each changed slot
+  uint32_t* mover_count;       // changed slots recorded (zeroed before the force pass)
   uint32_t* flags;             // [0] unused, [1] number of non-empty tiles this step
   // cell tiles (Morton order only; tile_bits == 0 disables them)
   int tile_bits;               // tiles of 2^tile_bits x 2^tile_bits cells
