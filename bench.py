@@ -288,7 +288,10 @@ def device_record(name, args, opts, stream, steps, warmup, with_e2e=True, world=
         best, ms = sphg.autotune(sprm if batched else [sprm], counts if batched else [n], x, y, vx, vy,
                                  base=opts, steps=5, stream=sptr)
         opts = best
-        tuned = {"ms_per_step": ms, "tile_bits": best.tile_bits, "resort": best.resort}
+        tuned = {"ms_per_step": ms, "tile_bits": best.tile_bits, "resort": best.resort,
+                 "block_threads": best.block_threads, "cell_pairs": best.cell_pairs,
+                 "searched": "tile_bits {off,3,4,5} x (untiled) re-sort {merge, full} x block {64,128,256} "
+                             "x particles per density thread {2 of a cell, 1}"}
     sim = sphg.Sim(sprm, counts, opts)
     sim.upload(x, y, vx, vy, stream=sptr)
     sim.preloop(stream=sptr)
@@ -318,8 +321,11 @@ def device_record(name, args, opts, stream, steps, warmup, with_e2e=True, world=
     tot = sum(pm)
     phases_out = {nm: {"ms": m, "share": m / tot if tot else 0.0} for nm, m in zip(names, pm)}
     sim.close()
+    cfg = workload_config(name, w, prm, n)
+    if opts.compute == sphg.LISTS:
+        cfg["compute"] = "lists"
     rec = {"value": value, "unit": UNIT, "steps": steps, "ms_per_step": total_ms / steps,
-           "config": workload_config(name, w, prm, n), "roofline": roofline_of(name, value, n),
+           "config": cfg, "roofline": roofline_of(name + ("_lists" if opts.compute == sphg.LISTS else ""), value, n),
            "resort_timed": rs, "gpu_launches": launches, "clocks": clk, "phases_ms": phases_out}
     if tuned:
         rec["autotune"] = tuned
@@ -492,7 +498,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     name = args.workload
     prec = sphg.SPLIT if WORKLOADS[name]["precision"] == "split" else sphg.PLAIN
-    opts = sphg.options(precision=prec, track_ids=0, use_graph=args.graph)
+    opts = sphg.options(precision=prec, track_ids=0, use_graph=args.graph, compute=args.compute)
     is_batch = WORKLOADS[name]["kind"] == "batch"
     rec, (w, prm, x, y, vx, vy) = device_record(name, args, opts, stream, args.steps, args.warmup,
                                                 world=world, tune=is_batch and args.graph == 1)
@@ -500,8 +506,10 @@ def run_gpu(args):
     if is_batch:
         tuned_opts = opts
         if "autotune" in rec:
-            tuned_opts = sphg.options(precision=prec, track_ids=0, use_graph=1,
-                                      tile_bits=rec["autotune"]["tile_bits"], resort=rec["autotune"]["resort"])
+            t = rec["autotune"]
+            tuned_opts = sphg.options(precision=prec, track_ids=0, use_graph=1, tile_bits=t["tile_bits"],
+                                      resort=t["resort"], block_threads=t["block_threads"],
+                                      cell_pairs=t["cell_pairs"])
         plain = plain_path(prm, w["counts"], x, y, vx, vy, tuned_opts, stream, max(3, min(args.steps, 20)))
         extra = {"plain_gpu_path": plain, "batched_vs_plain": rec["value"] / plain["value"]}
     nested = {}
@@ -510,6 +518,11 @@ def run_gpu(args):
             r1m, _ = device_record("dam_break_1m", args, sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1),
                                    stream, args.steps, args.warmup, with_e2e=False)
             nested["dam_break_1m"] = r1m
+        # the lists compute mode (CSR neighbour lists assembled every iteration) on the same dam break
+        rl, _ = device_record("dam_break_1m", args,
+                              sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1, compute="lists"),
+                              stream, args.steps, args.warmup, with_e2e=False)
+        nested["dam_break_1m_lists"] = rl
         if args.serve_seconds > 0:
             nested["serve"] = serve_record(args.serve_seconds, args.rate, args.serve_steps, args.budget_gb)
     if world > 1:
@@ -566,6 +579,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of CPU baseline sampling (0 = skip)")
+    ap.add_argument("--compute", default="sorted", choices=["sorted", "lists"],
+                    help="compute mode of the named workload (lists: CSR neighbour lists every iteration)")
     ap.add_argument("--graph", type=int, default=1,
                     help="1: every iteration replays a CUDA graph; 0: stream-launched kernels (for profilers)")
     ap.add_argument("--no-nested", action="store_true",

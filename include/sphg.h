@@ -102,12 +102,19 @@ typedef struct sphg_options {
   int32_t tile_bits;   /* density/force cell tiles of 2^b x 2^b cells staged in shared memory:
                           0 = default (off), 3..5 = that b (every instance in Morton order),
                           -1 = off (one thread per particle, L1-cached global loads) */
-  int32_t compute;     /* SPHG_COMPUTE_*; LISTS reads each iteration's list total back
-                          to size the lists, so it runs without CUDA graphs or cell tiles */
+  int32_t compute;     /* SPHG_COMPUTE_*; LISTS sizes its list buffer at the pre-loop
+                          (twice that iteration's total) and runs without cell tiles;
+                          lists that later outgrow it make sphg_download /
+                          sphg_diagnostics return SPHG_CAPACITY */
   int32_t resort;      /* 1 (default): when at most 8,192 particles changed cell since the
                           last iteration, re-sort by merging them into the unchanged
                           (already sorted) rest -- the same stable order as the full radix
                           sort, which runs otherwise; 0: full radix sort every iteration */
+  int32_t block_threads;/* threads per block of the density and force passes: 0 = default
+                          (128), 64, 128 or 256 */
+  int32_t cell_pairs;  /* density pass: 0 (default) one particle per thread; 1 one thread
+                          carries two particles of a cell (they share the stencil walk;
+                          the same results) */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;

@@ -257,7 +257,10 @@ sphg_status enqueue_full_sort(sphg_sim* s, cudaStream_t st, const uint32_t* skip
 }
 
 // Reorder + cell ranges, density, forces + integration (ev: events 3..5).
-sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev) {
+// size_lists: (lists mode) size the index buffer from this iteration's total
+// first -- a host synchronisation, done on the first iteration after an upload
+// (never inside a graph capture).
+sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev, bool size_lists = false) {
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
@@ -268,21 +271,31 @@ sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev) {
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
     // AssembleNeighborList: count, offsets, fill -- then density and forces over the lists
     SPHG_CUDA(sphg::launch_lists_count_scan(a, prec, s->csr_counts, s->csr_offs, s->csr_sums, st));
-    SPHG_CUDA(cudaMemcpyAsync(&s->csr_total, s->csr_sums + sphg::lists_scan_tiles(s->n), sizeof(int64_t),
-                              cudaMemcpyDeviceToHost, st));
-    SPHG_CUDA(cudaStreamSynchronize(st));
-    if (s->csr_total > s->csr_cap) {
-      const int64_t cap = s->csr_total + s->csr_total / 4 + 1024;
-      if (s->csr_idx) SPHG_CUDA(cudaFree(s->csr_idx));
-      s->csr_idx = nullptr;
-      s->csr_cap = 0;
-      cudaError_t e = cudaMalloc(&s->csr_idx, (size_t)cap * sizeof(uint32_t));
-      if (e != cudaSuccess)
-        return fail(SPHG_OOM, std::string("neighbour-list buffer: ") + cudaGetErrorString(e));
-      s->csr_cap = cap;
+    if (size_lists || !s->csr_idx) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      SPHG_CUDA(cudaStreamIsCapturing(st, &cs));
+      if (cs != cudaStreamCaptureStatusNone)
+        return fail(SPHG_INVALID_ARG, "lists mode: the neighbour-list buffer is sized before any graph capture");
+      SPHG_CUDA(cudaMemcpyAsync(&s->csr_total, s->csr_sums + sphg::lists_scan_tiles(s->n), sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, st));
+      SPHG_CUDA(cudaStreamSynchronize(st));
+      // twice this iteration's total (the lists of a compressing flow grow):
+      // later iterations run without a host synchronisation and report an
+      // overflow past it through the overflow word
+      const int64_t cap = 2 * s->csr_total + 1024;
+      if (cap > s->csr_cap) {
+        if (s->csr_idx) SPHG_CUDA(cudaFree(s->csr_idx));
+        s->csr_idx = nullptr;
+        s->csr_cap = 0;
+        s->drop_graphs();  // their kernels hold the old buffer
+        cudaError_t e = cudaMalloc(&s->csr_idx, (size_t)cap * sizeof(uint32_t));
+        if (e != cudaSuccess)
+          return fail(SPHG_OOM, std::string("neighbour-list buffer: ") + cudaGetErrorString(e));
+        s->csr_cap = cap;
+      }
     }
     const StepArgs b = s->args();
-    SPHG_CUDA(sphg::launch_lists_fill_packed(b, prec, s->csr_offs, s->csr_idx, s->csr_cap, st));
+    SPHG_CUDA(sphg::launch_lists_fill_packed(b, prec, s->csr_offs, s->csr_idx, s->csr_cap, s->flags + 8, st));
     SPHG_CUDA(sphg::launch_density(b, prec, st, true));
     if (ev) SPHG_CUDA(cudaEventRecord(ev[4], st));
     SPHG_CUDA(sphg::launch_force(b, prec, sphg::kForceIntegrate, st, true));
@@ -316,7 +329,7 @@ sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* 
   else if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->flags + 3, 0, sizeof(uint32_t), st));
   SPHG_TRY(enqueue_full_sort(s, st, inc ? s->flags + 3 : nullptr));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[2], st));
-  return enqueue_after_sort(s, st, ev);
+  return enqueue_after_sort(s, st, ev, first);
 }
 
 // The step header of the current state into the header slot (graph-capturable).
@@ -452,10 +465,13 @@ sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p) {
     return fail(SPHG_INVALID_ARG, "cell tiles need Morton order on every instance and tile_bits in 3..5");
   if (s->opt.compute != SPHG_COMPUTE_SORTED && s->opt.compute != SPHG_COMPUTE_LISTS)
     return fail(SPHG_INVALID_ARG, "unknown compute mode");
+  const int bt = s->opt.block_threads;
+  if (bt != 0 && bt != 64 && bt != 128 && bt != 256)
+    return fail(SPHG_INVALID_ARG, "block_threads must be 0 (default), 64, 128 or 256");
+  if (s->opt.cell_pairs < 0 || s->opt.cell_pairs > 1) return fail(SPHG_INVALID_ARG, "cell_pairs must be 0 or 1");
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
     if (tb > 0) return fail(SPHG_INVALID_ARG, "the lists compute mode runs without cell tiles");
     tb = -1;
-    s->opt.use_graph = 0;  // every iteration reads its list total back
   }
   s->tile_bits = tb > 0 ? tb : 0;
   // the tile kernels do not record which slots changed cell
@@ -648,6 +664,8 @@ void sphg_default_options(sphg_options* o) {
   o->tile_bits = 0;
   o->compute = SPHG_COMPUTE_SORTED;
   o->resort = 1;
+  o->block_threads = 0;
+  o->cell_pairs = 0;
 }
 
 const char* sphg_last_error_string(void) { return g_err.c_str(); }
@@ -714,8 +732,10 @@ sphg_status sphg_create_batch(int32_t ninst, const sphg_params* p, const int64_t
   if (st == SPHG_OK && s->n > 0 &&
       !host_stage(s, (size_t)s->n * (sizeof(float2) * 2 + sizeof(float4) + sizeof(float) + sizeof(uint32_t))))
     st = fail(SPHG_OOM, "pinned host staging");
-  if (st == SPHG_OK && s->n > 0 && s->opt.use_graph) st = build_graph(s);
-  if (st == SPHG_OK && s->n > 0 && s->opt.use_graph) st = build_graph(s, true);  // with step headers
+  // (lists mode: captured after the pre-loop has sized the list buffer)
+  const bool capture_now = s->opt.use_graph && s->opt.compute != SPHG_COMPUTE_LISTS;
+  if (st == SPHG_OK && s->n > 0 && capture_now) st = build_graph(s);
+  if (st == SPHG_OK && s->n > 0 && capture_now) st = build_graph(s, true);  // with step headers
   if (st != SPHG_OK) {
     destroy_impl(s);
     return st;
@@ -815,12 +835,15 @@ sphg_status sphg_step(sphg_sim* s, int64_t nsteps, void* stream) {
 // look-back (a wait that gave up) and the incremental re-sort's consistency
 // word.  Read at the synchronising calls; both stay set.
 static sphg_status device_errors(sphg_sim* s, cudaStream_t st) {
-  uint32_t w[2] = {0, 0};
+  uint32_t w[3] = {0, 0, 0};
   SPHG_CUDA(cudaMemcpyAsync(&w[0], sphg::sort_error_word(s->scratch), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaMemcpyAsync(&w[1], s->flags + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(&w[2], s->flags + 8, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
   if (w[0]) return fail(SPHG_TIMEOUT, "a radix-sort look-back wait gave up; the state is not valid");
   if (w[1]) return fail(SPHG_CUDA_ERROR, "inconsistent incremental re-sort record; the state is not valid");
+  if (w[2]) return fail(SPHG_CAPACITY, "lists mode: the neighbour lists outgrew their buffer (twice the pre-loop's "
+                                       "total); the state is not valid");
   return SPHG_OK;
 }
 

@@ -63,7 +63,8 @@ struct sphg_sim {
   uint32_t* tile_list = nullptr;
   uint32_t *nbr = nullptr, *ncount = nullptr;
   int nbr_slots = 0;
-  // lists mode: CSR of each iteration; the index buffer grows with the list total
+  // lists mode: CSR of each iteration; the index buffer is sized at the pre-loop
+  // (twice the list total then) and an overflow past it is reported
   int32_t* csr_counts = nullptr;
   int64_t *csr_offs = nullptr, *csr_sums = nullptr;
   uint32_t* csr_idx = nullptr;
@@ -128,11 +129,15 @@ struct sphg_sim {
     a.tile_list = tile_list;
     a.tile_count = flags + 1;
     a.force_batched = force_batched;
+    a.block = opt.block_threads > 0 ? opt.block_threads : 128;
+    a.cell_pairs = opt.cell_pairs > 0 ? 1 : 0;
     a.nbr = tile_bits ? nullptr : nbr;  // the tile kernels walk the stencil in both passes
     a.ncount = ncount;
     a.nbr_slots = nbr_slots;
     a.csr_offs = csr_offs;
     a.csr_idx = csr_idx;
+    a.csr_cap = csr_cap;
+    a.csr_overflow = flags + 8;
     a.keyS = keyTmp;
     a.merged = movers_on ? flags + 3 : nullptr;
     a.mover_mask = movers_on ? mmask : nullptr;
@@ -176,6 +181,8 @@ int instance_of(const sphg_sim* s, int64_t i);
 uint32_t morton_host(uint32_t x, uint32_t y);
 void demorton_host(uint32_t z, int& x, int& y);
 // One main-loop iteration on st; ev (6 events, optional) records the phase boundaries.
+// first: the iteration after an upload (cell keys computed; in lists mode the
+// index buffer is sized from this iteration's list total, a host synchronisation).
 sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false, cudaEvent_t* ev = nullptr);
 // Captures (once per layout) the CUDA graph of one iteration (header: followed
 // by its step header into the header slot).

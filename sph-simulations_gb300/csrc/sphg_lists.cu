@@ -50,10 +50,12 @@ __global__ void __launch_bounds__(kListThreads) lists_fill(StepArgs a, const int
 
 // Lists mode: the same walk, entries packed as j << 5 | tag (stencil offset and
 // periodic-wrap bit, read back by the density and force passes); at most cap
-// entries are written (the host sized the buffer from this iteration's total).
+// entries are written (the buffer was sized at the pre-loop), and a list that
+// runs past it sets *overflow, which the synchronising calls report.
 template <int PREC, bool BATCHED>
 __global__ void __launch_bounds__(kListThreads) lists_fill_packed(StepArgs a, const int64_t* offs,
-                                                                  uint32_t* idx, int64_t cap) {
+                                                                  uint32_t* idx, int64_t cap,
+                                                                  uint32_t* overflow) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const InstDesc d = inst_of<BATCHED>(a, i);
@@ -64,6 +66,7 @@ __global__ void __launch_bounds__(kListThreads) lists_fill_packed(StepArgs a, co
                                   if (o < cap) idx[o] = (j << 5) | tag;
                                   ++o;
                                 });
+  if (o > cap && overflow) *overflow = 1u;
 }
 
 // Exclusive scan of int32 counts into int64 offsets (offs[n] = total).
@@ -213,17 +216,17 @@ cudaError_t launch_lists_count_scan(const StepArgs& a, int precision, int32_t* c
 }
 
 cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int64_t* offs,
-                                     uint32_t* idx, int64_t cap, cudaStream_t st) {
+                                     uint32_t* idx, int64_t cap, uint32_t* overflow, cudaStream_t st) {
   const int64_t n = a.n;
   if (n == 0) return cudaSuccess;
   const unsigned g = (unsigned)((n + kListThreads - 1) / kListThreads);
   const bool batched = (a.ninst > 1 || a.force_batched);
   if (precision) {
-    if (batched) lists_fill_packed<1, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
-    else lists_fill_packed<1, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+    if (batched) lists_fill_packed<1, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap, overflow);
+    else lists_fill_packed<1, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap, overflow);
   } else {
-    if (batched) lists_fill_packed<0, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
-    else lists_fill_packed<0, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap);
+    if (batched) lists_fill_packed<0, true><<<g, kListThreads, 0, st>>>(a, offs, idx, cap, overflow);
+    else lists_fill_packed<0, false><<<g, kListThreads, 0, st>>>(a, offs, idx, cap, overflow);
   }
   return cudaGetLastError();
 }

@@ -77,13 +77,12 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- reorder + cell ranges
-// kReorderSlots slots per thread, strided by the block size (coalesced), their
-// keys loaded before any is used.
+// kReorderSlots consecutive slots per thread: their keys in one 16-byte load,
+// the neighbouring keys of the first and last from the adjacent lanes.
 constexpr int kReorderSlots = 4;
 
 __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint32_t k, uint32_t kprev,
                                              uint32_t knext, bool gather, uint32_t ep) {
-  a.keyA[i] = k;
   if (gather) {  // after a full sort (a merge scattered the state already)
     const uint32_t src = a.perm[i];
     a.posA[i] = a.posB[src];
@@ -110,24 +109,36 @@ __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint3
 }
 
 __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
-  const int64_t base = (int64_t)blockIdx.x * (kThreads * kReorderSlots) + threadIdx.x;
-  uint32_t k[kReorderSlots], kp[kReorderSlots], kn[kReorderSlots];
+  const int64_t base = ((int64_t)blockIdx.x * kThreads + threadIdx.x) * kReorderSlots;
+  const int lane = threadIdx.x & 31;
+  const bool whole = base + kReorderSlots <= a.n;  // keys buffers are 256-byte aligned: base is 16-byte aligned
+  uint32_t k[kReorderSlots];
+  if (whole) {
+    const uint4 v = *reinterpret_cast<const uint4*>(a.keyS + base);
+    k[0] = v.x; k[1] = v.y; k[2] = v.z; k[3] = v.w;
+  } else {
 #pragma unroll
-  for (int u = 0; u < kReorderSlots; ++u) {
-    const int64_t i = base + (int64_t)u * kThreads;
-    k[u] = kp[u] = kn[u] = kNoIndex;
-    if (i < a.n) {
-      k[u] = a.keyS[i];
-      kp[u] = i > 0 ? a.keyS[i - 1] : kNoIndex;
-      kn[u] = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;
-    }
+    for (int u = 0; u < kReorderSlots; ++u) k[u] = base + u < a.n ? a.keyS[base + u] : kNoIndex;
   }
+  uint32_t kp = __shfl_up_sync(0xffffffffu, k[kReorderSlots - 1], 1);
+  uint32_t kn = __shfl_down_sync(0xffffffffu, k[0], 1);
+  if (lane == 0) kp = (base > 0 && base - 1 < a.n) ? a.keyS[base - 1] : kNoIndex;
+  if (lane == 31) kn = base + kReorderSlots < a.n ? a.keyS[base + kReorderSlots] : kNoIndex;
+  if (base >= a.n) return;
   const bool gather = !(a.merged && *a.merged);
   const uint32_t ep = *a.epoch;
+  if (whole) {
+    *reinterpret_cast<uint4*>(a.keyA + base) = make_uint4(k[0], k[1], k[2], k[3]);
+  } else {
+#pragma unroll
+    for (int u = 0; u < kReorderSlots; ++u)
+      if (base + u < a.n) a.keyA[base + u] = k[u];
+  }
 #pragma unroll
   for (int u = 0; u < kReorderSlots; ++u) {
-    const int64_t i = base + (int64_t)u * kThreads;
-    if (i < a.n) reorder_slot(a, i, k[u], kp[u], kn[u], gather, ep);
+    const int64_t i = base + u;
+    if (i < a.n)
+      reorder_slot(a, i, k[u], u ? k[u - 1] : kp, u + 1 < kReorderSlots ? k[u + 1] : kn, gather, ep);
   }
 }
 
@@ -150,8 +161,8 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
   }
 }
 
-template <int PREC, bool BATCHED, bool CSR>
-__global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
+template <int PREC, bool BATCHED, bool CSR, int T = kThreads>
+__global__ void __launch_bounds__(T) step_density(StepArgs a) {
   cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -164,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   const float inv_h2 = d.inv_h2;
   if constexpr (CSR) {
     // MPListsForceComputation::ApproximateDensity: the list in its order, self included
-    const int64_t b = a.csr_offs[i], e = a.csr_offs[i + 1];
+    const int64_t b = min(a.csr_offs[i], a.csr_cap), e = min(a.csr_offs[i + 1], a.csr_cap);
     for (int64_t q = b; q < e; ++q) {
       const uint32_t ent = __ldg(a.csr_idx + q);
       float dx, dy;
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
       S.add(t * t * t);
     }
   } else {
-    __shared__ uint4 s_cells[9][kThreads];  // per thread: its non-empty stencil cells
+    __shared__ uint4 s_cells[9][T];  // per thread: its non-empty stencil cells
     uint32_t* __restrict__ nbr = a.nbr;
     const uint32_t slots = (uint32_t)a.nbr_slots;
     const size_t n = (size_t)a.n;
@@ -320,6 +331,255 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
   reinterpret_cast<float2*>(a.velpA + i)[1] = make_float2(P, inv);
 }
 
+// ---------------------------------------------------------------- density, two particles of a cell per thread
+// The same computation as step_density's flattened stencil walk, arranged so
+// that one thread carries two particles of one cell: they share the cell's
+// stencil, its range loads, its queue of non-empty cells and every candidate's
+// position load, while each keeps its own sum, neighbour record and self test
+// -- so every particle visits the same candidates in the same order with the
+// same arithmetic as in step_density (bit-identical results).  A block takes
+// 256 consecutive slots, splits each run of equal keys (a cell, or the part of
+// it inside the block) into pairs from its first slot, and hands the pairs
+// and the odd particles out to its threads in slot order.
+// slots per block: two per thread
+
+
+// One particle's running state of the walk.
+template <int PREC>
+struct WalkAcc {
+  typename std::conditional<PREC == 1, CSum, PSum>::type S;
+  uint32_t cnt = 0;
+  uint32_t* rp = nullptr;  // next record slot: nbr[cnt * n + i]
+};
+
+// Rare: pairs of particle pi inside the FP64 band around h^2, over the same
+// queued cells in the same order (step_density's second pass).
+template <int PREC, int T, class Acc>
+__device__ __forceinline__ void band_pass(const InstDesc& d, const float2* __restrict__ pos,
+                                          const uint4 (*cells)[T], int nseg, int tid, float2 pi,
+                                          uint32_t self, Acc& A, uint32_t slots, size_t n, bool record) {
+  const float h2_lo = d.h2_lo, h2_hi = d.h2_hi, inv_h2 = d.inv_h2;
+#pragma unroll 1
+  for (int s = 0; s < nseg; ++s) {
+    const uint4 w = cells[s][tid];
+    const uint32_t tag = w.x & 31u;
+    if (PREC == 0 && (tag & 16u)) continue;
+    const int c1 = (int)(tag / 3) - 1, c2 = (int)(tag % 3) - 1;
+    const float sx = __uint_as_float(w.z), sy = __uint_as_float(w.w);
+    for (uint32_t e = w.x; e != w.y; e += 32u) {
+      const float2 pj = __ldg(pos + (e >> 5));
+      const float dx = (pi.x - pj.x) - sx;
+      const float dy = (pi.y - pj.y) - sy;
+      const float r2 = fmaf(dx, dx, dy * dy);
+      if (r2 >= h2_lo && r2 <= h2_hi && pair_inside<PREC>(d, pi, pj, c1, c2, r2)) {
+        const float t = fmaf(-r2, inv_h2, 1.0f);
+        A.S.add(t * t * t);
+        if (record && (e >> 5) != self) {
+          if (A.cnt < slots) *A.rp = e;
+          A.rp += n;
+          ++A.cnt;
+        }
+      }
+    }
+  }
+}
+
+template <int PREC>
+__device__ __forceinline__ void density_epilogue(const StepArgs& a, const InstDesc& d, int64_t i,
+                                                 const typename std::conditional<PREC == 1, CSum, PSum>::type& S) {
+  float rho, drho;
+  if constexpr (PREC == 1) {
+    rho = d.wd * S.value();
+    drho = fmaf(d.wd, S.s, -d.rho0) + d.wd * S.c;
+  } else {
+    rho = d.wd * S.value();
+    drho = rho - d.rho0;
+  }
+  const float inv = 1.0f / rho;
+  const float P = d.k * drho * inv * inv;
+  a.rho[i] = rho;
+  reinterpret_cast<float2*>(a.velpA + i)[1] = make_float2(P, inv);
+}
+
+template <int PREC, bool BATCHED, int T = kThreads>
+__global__ void __launch_bounds__(T) step_density_pairs(StepArgs a) {
+  constexpr int kPairSlots = 2 * T;
+  cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
+  __shared__ uint32_t s_key[kPairSlots];
+  __shared__ uint16_t s_chunk[kPairSlots];  // offset of each pair's (or odd particle's) first slot | partner << 15
+  __shared__ uint32_t s_wmax[T / 32], s_wcnt[T / 32];
+  __shared__ uint4 s_cells[9][T];   // per thread: the non-empty stencil cells of its cell
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t b0 = (int64_t)blockIdx.x * kPairSlots;
+  const int nb = (int)min((int64_t)kPairSlots, a.n - b0);
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int o = u * T + tid;
+    s_key[o] = o < nb ? __ldg(a.keyA + b0 + o) : kNoIndex;
+  }
+  __syncthreads();
+  // runs of equal keys inside the block: start of each slot's run by a max-scan
+  // (thread t holds offsets 2t, 2t+1), pairs counted from the run's start
+  const int o0 = 2 * tid, o1 = o0 + 1;
+  const uint32_t k0 = s_key[o0], k1 = s_key[o1];
+  const int st0 = (o0 == 0 || s_key[o0 - 1] != k0) ? o0 : 0;
+  const int st1 = (k1 != k0) ? o1 : 0;
+  int m = max(st0, st1);
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, m, d);
+    if (lane >= d) m = max(m, y);
+  }
+  if (lane == 31) s_wmax[warp] = m;
+  int excl = __shfl_up_sync(0xffffffffu, m, 1);
+  if (lane == 0) excl = 0;
+  __syncthreads();
+  for (int w = 0; w < warp; ++w) excl = max(excl, (int)s_wmax[w]);
+  const int rs0 = max(excl, st0), rs1 = max(rs0, st1);
+  const bool lead0 = o0 < nb && ((o0 - rs0) & 1) == 0;
+  const bool lead1 = o1 < nb && ((o1 - rs1) & 1) == 0;
+  const bool part0 = lead0 && o1 < nb && k1 == k0;
+  const bool part1 = lead1 && o1 + 1 < nb && s_key[o1 + 1] == k1;
+  const uint32_t c = (lead0 ? 1u : 0u) + (lead1 ? 1u : 0u);
+  uint32_t x = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) s_wcnt[warp] = x;
+  __syncthreads();
+  uint32_t at = x - c, nchunks = 0;
+  for (int w = 0; w < T / 32; ++w) {
+    if (w < warp) at += s_wcnt[w];
+    nchunks += s_wcnt[w];
+  }
+  if (lead0) s_chunk[at++] = (uint16_t)(o0 | (part0 ? 0x8000 : 0));
+  if (lead1) s_chunk[at] = (uint16_t)(o1 | (part1 ? 0x8000 : 0));
+  __syncthreads();
+
+  uint32_t* __restrict__ nbr = a.nbr;
+  const uint32_t slots = (uint32_t)a.nbr_slots;
+  const size_t n = (size_t)a.n;
+  const bool record = nbr != nullptr;
+  const float2* __restrict__ pos = a.posA;
+  for (uint32_t q = tid; q < nchunks; q += T) {
+    const uint32_t ce = s_chunk[q];
+    const int off = (int)(ce & 0x7fffu);
+    const bool hasB = (ce >> 15) != 0;
+    const int64_t iA = b0 + off, iB = hasB ? iA + 1 : iA;
+    typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, iA);
+    if (BATCHED && !d.active) continue;  // a finished served instance
+    const uint32_t key = s_key[off];
+    const float2 pA = pos[iA], pB = pos[iB];
+    const float inv_h2 = d.inv_h2;
+    int cx, cy;
+    const uint32_t code = key - d.cell_base;
+    decode_code(d, code, cx, cy);
+    const uint32_t ep = *a.epoch;
+    uint32_t cs[9], valid, wrapmask;
+    stencil_keys(d, code, cx, cy, cs, valid, wrapmask);
+    uint4 r[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r[k] = ((valid >> k) & 1u) ? __ldg(a.ranges + cs[k]) : make_uint4(0, 0, 0, 0);
+    int nseg = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      if (r[k].z == ep && r[k].y > r[k].x) {
+        const int c1 = k / 3 - 1, c2 = k % 3 - 1;
+        const uint32_t tag = (uint32_t)k | ((PREC == 0 && ((wrapmask >> k) & 1u)) ? 16u : 0u);
+        const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
+        const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
+        s_cells[nseg][tid] = make_uint4((r[k].x << 5) | tag, (r[k].y << 5) | tag, __float_as_uint(shx),
+                                        __float_as_uint(shy));
+        ++nseg;
+      }
+    }
+    const float h2_lo = d.h2_lo, h2_hi = d.h2_hi;
+    WalkAcc<PREC> A, B;
+    A.rp = record ? nbr + iA : nullptr;
+    B.rp = record ? nbr + iB : nullptr;
+    bool border = false;
+    if (PREC == 1) {  // own terms W(0) first (plain sums keep the walk's order)
+      A.S.add(1.0f);
+      B.S.add(1.0f);
+    }
+    if (nseg > 0) {  // always: the particles' own cell holds them
+      uint4 w = s_cells[0][tid];
+      int qq = 1;
+      uint32_t jj = w.x, je = w.y;
+      float shx = __uint_as_float(w.z), shy = __uint_as_float(w.w);
+      float2 pj = __ldg(pos + (jj >> 5));
+      while (true) {
+        uint32_t jn = jj + 32u, jen = je;
+        float shxn = shx, shyn = shy;
+        bool more = true;
+        if (jn == je) {
+          if (qq == nseg) {
+            more = false;
+          } else {
+            w = s_cells[qq][tid];
+            ++qq;
+            jn = w.x;
+            jen = w.y;
+            shxn = __uint_as_float(w.z);
+            shyn = __uint_as_float(w.w);
+          }
+        }
+        const float2 pn = __ldg(pos + ((more ? jn : jj) >> 5));  // one candidate ahead
+        const uint32_t j = jj >> 5;
+        float dxa = (pA.x - pj.x) - shx, dya = (pA.y - pj.y) - shy;
+        float dxb = (pB.x - pj.x) - shx, dyb = (pB.y - pj.y) - shy;
+        float r2a, r2b;
+        bool ina, inb;
+        if (PREC == 0 && (jj & 16u)) {  // plain positions reached through the periodic boundary
+          ina = wrapped_pair(d, pA, pj, dxa, dya);
+          inb = wrapped_pair(d, pB, pj, dxb, dyb);
+          r2a = fmaf(dxa, dxa, dya * dya);
+          r2b = fmaf(dxb, dxb, dyb * dyb);
+        } else {
+          r2a = fmaf(dxa, dxa, dya * dya);
+          r2b = fmaf(dxb, dxb, dyb * dyb);
+          ina = r2a < h2_lo;
+          inb = r2b < h2_lo;
+          border |= (!ina && r2a <= h2_hi) || (!inb && r2b <= h2_hi);
+        }
+        const bool oa = j != (uint32_t)iA, ob = j != (uint32_t)iB;
+        const float ta = fmaf(-r2a, inv_h2, 1.0f), tb = fmaf(-r2b, inv_h2, 1.0f);
+        A.S.add_fast((PREC == 1 ? ina && oa : ina) ? ta * ta * ta : 0.0f);
+        B.S.add_fast((PREC == 1 ? inb && ob : inb) ? tb * tb * tb : 0.0f);
+        const bool ra = ina && oa && record, rb = hasB && inb && ob && record;
+        if (ra && A.cnt < slots) {
+          *A.rp = jj;
+          A.rp += n;
+        }
+        if (rb && B.cnt < slots) {
+          *B.rp = jj;
+          B.rp += n;
+        }
+        A.cnt += ra ? 1u : 0u;
+        B.cnt += rb ? 1u : 0u;
+        if (!more) break;
+        jj = jn;
+        je = jen;
+        shx = shxn;
+        shy = shyn;
+        pj = pn;
+      }
+    }
+    if (border) {
+      band_pass<PREC, T>(d, pos, s_cells, nseg, tid, pA, (uint32_t)iA, A, slots, n, record);
+      if (hasB) band_pass<PREC, T>(d, pos, s_cells, nseg, tid, pB, (uint32_t)iB, B, slots, n, record);
+    }
+    if (record) a.ncount[iA] = A.cnt;
+    density_epilogue<PREC>(a, d, iA, A.S);
+    if (hasB) {
+      if (record) a.ncount[iB] = B.cnt;
+      density_epilogue<PREC>(a, d, iB, B.S);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- forces (+ integration)
 // The pairs are the neighbours the density pass recorded (j << 5 | stencil
 // tag per entry); a particle with more than the recorded slots walks the
@@ -328,14 +588,17 @@ __global__ void __launch_bounds__(kThreads) step_density(StepArgs a) {
 #define SPHG_FORCE_BATCH 4
 #endif
 constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered together
+#ifndef SPHG_FORCE_TAIL
+#define SPHG_FORCE_TAIL 1
+#endif
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
 
-// Eight blocks per SM (64 registers) for one instance; the batched variants
+// 1,024 threads per SM (64 registers) for one instance; the batched variants
 // are left to the compiler (their instance lookup needs more registers).
-template <int PREC, bool BATCHED, int MODE, bool CSR>
-__global__ void __launch_bounds__(kThreads, BATCHED ? 0 : 8) step_force(StepArgs a) {
+template <int PREC, bool BATCHED, int MODE, bool CSR, int T = kThreads>
+__global__ void __launch_bounds__(T, BATCHED ? 0 : 1024 / T) step_force(StepArgs a) {
   // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
   // recorded neighbours: one shared-memory load per pair instead of decoding k
   __shared__ float2 unit[16];
@@ -415,11 +678,11 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
   auto pair = [&](uint32_t j, float dx, float dy) { pair_v(__ldg(velp + j), dx, dy); };
   int cx, cy;
   const uint32_t cnt = CSR ? 0u : (a.nbr ? a.ncount[i] : 0xffffffffu);
-  if (CSR) {
+  if constexpr (CSR) {
     // MPListsForceComputation::ComputeForces: the list in its order (self skipped:
     // its pressure term is excluded by r > TOL and its viscosity term is zero)
     decode_code(d, key - d.cell_base, cx, cy);
-    const int64_t b = a.csr_offs[i], e = a.csr_offs[i + 1];
+    const int64_t b = min(a.csr_offs[i], a.csr_cap), e = min(a.csr_offs[i + 1], a.csr_cap);
     for (int64_t q = b; q < e; ++q) {
       const uint32_t ent = __ldg(a.csr_idx + q);
       const uint32_t j = ent >> 5;
@@ -428,29 +691,32 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
       entry_vec<PREC>(d, pi, __ldg(a.posA + j), ent, dx, dy);
       pair(j, dx, dy);
     }
-  } else if (cnt <= (uint32_t)a.nbr_slots) {
+  } else if (cnt <= (uint32_t)a.nbr_slots) {  // (not CSR: the lists mode has no record)
     // the density pass recorded this particle's neighbours (stencil order)
     decode_code(d, key - d.cell_base, cx, cy);
     const size_t n = (size_t)a.n;
     // kForceBatch neighbours at a time, their gathers in flight together.  The
-    // lanes of a warp all run the warp's largest count rounded up to whole
-    // batches; a lane's missing entries are the particle itself (stencil cell
-    // 4, no shift), whose pair term is exactly zero (r = 0, v_j = v_i).
+    // lanes of a warp all run the warp's largest count: whole batches, then
+    // (SPHG_FORCE_TAIL) a batch of two and a single one for the rest; a lane's
+    // missing entries are the particle itself (stencil cell 4, no shift), whose
+    // pair term is exactly zero (r = 0, v_j = v_i), so the sums are the same
+    // whatever the batching.
     const uint32_t wmax = __reduce_max_sync(__activemask(), cnt);
     const uint32_t self_e = ((uint32_t)i << 5) | 4u;
-    for (uint32_t q = 0; q < wmax; q += kForceBatch) {
-      uint32_t e[kForceBatch];
-      float2 pj[kForceBatch];
-      float4 vj[kForceBatch];
+    auto batch = [&](auto width, uint32_t q) {
+      constexpr int B = decltype(width)::value;
+      uint32_t e[B];
+      float2 pj[B];
+      float4 vj[B];
 #pragma unroll
-      for (int u = 0; u < kForceBatch; ++u) e[u] = q + u < cnt ? __ldg(a.nbr + (q + u) * n + i) : self_e;
+      for (int u = 0; u < B; ++u) e[u] = q + u < cnt ? __ldg(a.nbr + (q + u) * n + i) : self_e;
 #pragma unroll
-      for (int u = 0; u < kForceBatch; ++u) {
+      for (int u = 0; u < B; ++u) {
         pj[u] = __ldg(a.posA + (e[u] >> 5));
         vj[u] = __ldg(velp + (e[u] >> 5));
       }
 #pragma unroll
-      for (int u = 0; u < kForceBatch; ++u) {
+      for (int u = 0; u < B; ++u) {
         float dx, dy;
         if (PREC == 1) {  // split: the offsets moved into one cell frame by the tag's stencil offset
           const float2 o = unit[e[u] & 15u];
@@ -461,7 +727,18 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
         }
         pair_v(vj[u], dx, dy);
       }
+    };
+#if SPHG_FORCE_TAIL
+    uint32_t q = 0;
+    for (; q + kForceBatch <= wmax; q += kForceBatch) batch(std::integral_constant<int, kForceBatch>(), q);
+    if (q + 2 <= wmax) {
+      batch(std::integral_constant<int, 2>(), q);
+      q += 2;
     }
+    if (q < wmax) batch(std::integral_constant<int, 1>(), q);
+#else
+    for (uint32_t q = 0; q < wmax; q += kForceBatch) batch(std::integral_constant<int, kForceBatch>(), q);
+#endif
   } else {
     // more neighbours than the density pass could record (or no record): the
     // stencil walk, pairs in the walk's order
@@ -804,13 +1081,52 @@ cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The sorted-mode density pass with T-thread blocks: two particles of a cell
+// per thread (pairs) or one.
+template <int T>
+static cudaError_t density_sorted(const StepArgs& a, int precision, bool b, bool pairs, cudaStream_t s) {
+  if (pairs) {
+    const dim3 g(blocks_for(a.n, 2 * T)), t(T);
+    if (precision) return b ? launch_pdl(step_density_pairs<1, true, T>, g, t, 0, s, a)
+                            : launch_pdl(step_density_pairs<1, false, T>, g, t, 0, s, a);
+    return b ? launch_pdl(step_density_pairs<0, true, T>, g, t, 0, s, a)
+             : launch_pdl(step_density_pairs<0, false, T>, g, t, 0, s, a);
+  }
+  const dim3 g(blocks_for(a.n, T)), t(T);
+  if (precision) return b ? launch_pdl(step_density<1, true, false, T>, g, t, 0, s, a)
+                          : launch_pdl(step_density<1, false, false, T>, g, t, 0, s, a);
+  return b ? launch_pdl(step_density<0, true, false, T>, g, t, 0, s, a)
+           : launch_pdl(step_density<0, false, false, T>, g, t, 0, s, a);
+}
+
 cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s, bool csr) {
   if (a.n == 0) return cudaSuccess;
-  const unsigned g = blocks_for(a.n, kThreads);
   const bool b = (a.ninst > 1 || a.force_batched);
-  if (csr) SPHG_DISPATCH2(precision, b, step_density, , true);
-  else SPHG_DISPATCH2_PDL(precision, b, step_density, , false);
+  cudaError_t e;
+  if (csr) {
+    const unsigned g = blocks_for(a.n, kThreads);
+    SPHG_DISPATCH2(precision, b, step_density, , true);
+    return cudaGetLastError();
+  }
+  // the pairs kernel needs the neighbour record (below 2^27 particles)
+  const bool pairs = a.cell_pairs && a.n < ((int64_t)1 << 27);
+  switch (a.block) {
+    case 64: e = density_sorted<64>(a, precision, b, pairs, s); break;
+    case 256: e = density_sorted<256>(a, precision, b, pairs, s); break;
+    default: e = density_sorted<kThreads>(a, precision, b, pairs, s); break;
+  }
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+// The sorted-mode force + integration pass with T-thread blocks.
+template <int T>
+static cudaError_t force_sorted(const StepArgs& a, int precision, bool b, cudaStream_t s) {
+  const dim3 g(blocks_for(a.n, T)), t(T);
+  if (precision) return b ? launch_pdl(step_force<1, true, kForceIntegrate, false, T>, g, t, 0, s, a)
+                          : launch_pdl(step_force<1, false, kForceIntegrate, false, T>, g, t, 0, s, a);
+  return b ? launch_pdl(step_force<0, true, kForceIntegrate, false, T>, g, t, 0, s, a)
+           : launch_pdl(step_force<0, false, kForceIntegrate, false, T>, g, t, 0, s, a);
 }
 
 cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s, bool csr) {
@@ -820,9 +1136,16 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
   if (csr) {
     if (mode == kForceOnly) SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, true);
     else SPHG_DISPATCH2(precision, b, step_force, , kForceIntegrate, true);
+  } else if (mode == kForceOnly) {
+    SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, false);
   } else {
-    if (mode == kForceOnly) SPHG_DISPATCH2(precision, b, step_force, , kForceOnly, false);
-    else SPHG_DISPATCH2_PDL(precision, b, step_force, , kForceIntegrate, false);
+    cudaError_t e;
+    switch (a.block) {
+      case 64: e = force_sorted<64>(a, precision, b, s); break;
+      case 256: e = force_sorted<256>(a, precision, b, s); break;
+      default: e = force_sorted<kThreads>(a, precision, b, s); break;
+    }
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }

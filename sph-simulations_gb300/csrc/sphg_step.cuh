@@ -17,6 +17,8 @@ struct StepArgs {
   int ninst;
   int track_ids;
   int force_batched;           // 1: per-instance descriptor kernels even for one instance
+  int block;                   // threads per block of the density and force passes (64, 128, 256)
+  int cell_pairs;              // 1: the density pass carries two particles of a cell per thread
   InstDesc d0;                 // copy of desc[0] (single-instance fast path)
   const InstDesc* desc;        // [ninst]
   const int32_t* begins;       // [ninst]
@@ -42,6 +44,8 @@ struct StepArgs {
   int nbr_slots;
   const int64_t* csr_offs;     // [n+1] CSR neighbour lists of this iteration (lists mode)
   const uint32_t* csr_idx;     // j << 5 | tag entries, self included, list order
+  int64_t csr_cap;             // entries csr_idx holds (the passes read no further)
+  uint32_t* csr_overflow;      // set by the fill when the lists exceed csr_cap
   const uint32_t* merged;      // non-null and set: this iteration's merge scattered the state (reorder: ranges only)
   uint32_t* mover_mask;        // [ceil(n/32)] force pass: bit per slot whose key changed (or null)
   unsigned long long* mover_list;  // [kMoverCap] force pass: key << 32 | slot of each changed slot
@@ -68,7 +72,7 @@ int lists_scan_tiles(int64_t n);
 cudaError_t launch_lists_count_scan(const StepArgs& a, int precision, int32_t* counts, int64_t* offs,
                                     int64_t* sums, cudaStream_t st);
 cudaError_t launch_lists_fill_packed(const StepArgs& a, int precision, const int64_t* offs,
-                                     uint32_t* idx, int64_t cap, cudaStream_t st);
+                                     uint32_t* idx, int64_t cap, uint32_t* overflow, cudaStream_t st);
 // Per-instance diagnostics in one launch: float-float partials per (chunk,
 // instance) block, then the last block of an instance (ticket counter) sums them
 // in a fixed order; out[6*inst + {0..5}] = E_k, max|v|^2, inside, sum m vx,

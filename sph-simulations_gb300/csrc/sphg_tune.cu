@@ -1,9 +1,11 @@
 // sphg_tune.cu -- the autotuner: picks the launch configuration of a workload
 // by timing each candidate on the workload itself.
 //
-// Candidates: the cell-block shape (no tiles -- one thread per particle --, or
-// Morton tiles of 2^b x 2^b cells staged in shared memory, b = 3..5; tiles
-// need every instance in Morton order) crossed with the re-sort strategy
+// Candidates: the cell-block shape (no tiles, or Morton tiles of 2^b x 2^b
+// cells staged in shared memory, b = 3..5; tiles need every instance in Morton
+// order); without tiles, the particles per thread of the density pass (two of
+// a cell sharing the stencil walk, or one), the threads per block of the
+// density and force passes (64, 128, 256) and the re-sort strategy
 // (incremental merge of the particles that changed cell, or the full radix
 // sort every iteration).  Each candidate gets its own handle with the caller's
 // state, runs the pre-loop and a few warm-up iterations, then `steps` timed
@@ -77,12 +79,29 @@ extern "C" sphg_status sphg_autotune(int32_t ninst, const sphg_params* p, const 
   SPHG_CUDA(cudaEventCreate(&e1));
   Tuned win{b, -1.0};
   sphg_status res = SPHG_OK;
+  struct Cand {
+    int tb, resort, block, pairs;
+  };
+  std::vector<Cand> cands;
   for (int tb : tiles) {
-    for (int resort : {1, 0}) {
-      if (tb > 0 && resort) continue;  // the tile kernels do not record cell changes
+    if (tb > 0) {  // the tile kernels do not record cell changes; their blocks are their own
+      cands.push_back({tb, 0, 0, 0});
+      continue;
+    }
+    for (int resort : {1, 0})
+      for (int block : {128, 64, 256})
+        for (int pairs : {0, 1}) {
+          if (b.compute == SPHG_COMPUTE_LISTS && pairs) continue;  // lists mode: no stencil walk in the density
+          cands.push_back({tb, resort, block, pairs});
+        }
+  }
+  for (const Cand& cd : cands) {
+    {
       sphg_options o = b;
-      o.tile_bits = tb;
-      o.resort = resort;
+      o.tile_bits = cd.tb;
+      o.resort = cd.resort;
+      o.block_threads = cd.block;
+      o.cell_pairs = cd.pairs;
       sphg_sim* s = nullptr;
       sphg_status st2 = sphg_create_batch(ninst, p, counts, &o, &s);
       if (st2 == SPHG_OK) st2 = sphg_upload(s, x, y, vx, vy, stream);

@@ -12,7 +12,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libsphg.so")
+# SPHG_LIB: another build of the library (for comparing builds side by side)
+LIB_PATH = os.environ.get("SPHG_LIB") or os.path.join(HERE, "libsphg.so")
 
 OK, INVALID_ARG, OOM, NONFINITE, TIMEOUT, CUDA_ERROR, CAPACITY, NOT_READY = range(8)
 ORDER = {"morton": 0, "rowmajor": 1}
@@ -56,7 +57,8 @@ def lattice(x0, y0, dx, dy, nx, ny, jitter=0.0, seed=0, velocity=VEL_ZERO, u0=0.
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
-                ("compute", ctypes.c_int32), ("resort", ctypes.c_int32)]
+                ("compute", ctypes.c_int32), ("resort", ctypes.c_int32),
+                ("block_threads", ctypes.c_int32), ("cell_pairs", ctypes.c_int32)]
 
 
 _lib = None
@@ -165,11 +167,16 @@ def params(**kw):
     return p
 
 
-def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None, resort=None):
+def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None, resort=None,
+            block_threads=None, cell_pairs=None):
     o = Options()
     lib().sphg_default_options(ctypes.byref(o))
     if resort is not None:
         o.resort = int(resort)
+    if block_threads is not None:
+        o.block_threads = int(block_threads)
+    if cell_pairs is not None:
+        o.cell_pairs = int(cell_pairs)
     o.precision = precision
     o.track_ids = track_ids
     o.use_graph = use_graph

@@ -642,6 +642,69 @@ def test_lists_mode_steps_match_oracle_and_sorted_mode(prec, order):
     srt.close()
 
 
+def test_lists_mode_graph_equals_stream_launches():
+    """Lists mode replays a CUDA graph per iteration (the list buffer is sized at
+    the pre-loop, no per-iteration host synchronisation): the same bits as the
+    stream-launched iterations."""
+    S = _sphg()
+    x, y, vx, vy = jittered(48, 40, 0.005, seed=22, vel=0.3)
+    kw = dict(order="morton", h=0.0065, dt=1e-5, lo=(0, 0), hi=(0.4, 0.3))
+    out = []
+    for graph in (1, 0):
+        sim = S.Sim(S.params(**kw), len(x), S.options(precision=S.SPLIT, compute="lists", use_graph=graph))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        sim.step(12)
+        out.append(sim.download())
+        sim.close()
+    for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
+        assert (out[0][f] == out[1][f]).all(), f
+
+
+def test_lists_mode_reports_lists_outgrowing_their_buffer():
+    """A collapsing cloud: isolated particles (the pre-loop's lists hold only
+    each particle itself) driven together until every particle has four
+    neighbours -- more than the buffer sized at the pre-loop (twice that
+    total): the overflow is reported as SPHG_CAPACITY, nothing is written past
+    the buffer."""
+    S = _sphg()
+    h = 0.005
+    g = (np.arange(64) - 31.5) * 2 * h + 0.5
+    x, y = [a.ravel().astype(np.float32).astype(np.float64) for a in np.meshgrid(g, g, indexing="xy")]
+    vx, vy = -300.0 * (x - 0.5), -300.0 * (y - 0.5)
+    kw = dict(order="morton", h=h, dt=1e-4, lo=(0, 0), hi=(1, 1), gy=0.0)
+    sim = S.Sim(S.params(**kw), len(x), S.options(compute="lists"))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    sim.step(35)
+    with pytest.raises(S.SphgError) as e:
+        sim.download()
+    assert e.value.status == S.CAPACITY
+    sim.close()
+
+
+@pytest.mark.parametrize("opt", [dict(cell_pairs=1), dict(block_threads=64), dict(block_threads=256),
+                                 dict(cell_pairs=1, block_threads=64)])
+def test_launch_shapes_give_identical_results(opt):
+    """The autotuner's launch shapes (threads per block, two particles of a cell
+    per density thread) visit the same pairs in the same order: the same bits."""
+    S = _sphg()
+    inst = _instances()
+    prms = [S.params(**i[0]) for i in inst]
+    counts = [len(i[1]) for i in inst]
+    cat = [np.concatenate([i[k] for i in inst]) for k in (1, 2, 3, 4)]
+    out = []
+    for o in ({}, opt):
+        b = S.Sim(prms, counts, S.options(precision=S.SPLIT, **o))
+        b.upload(*cat)
+        b.preloop()
+        b.step(20)
+        out.append(b.download())
+        b.close()
+    for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
+        assert (out[0][f] == out[1][f]).all(), f
+
+
 def test_lists_mode_periodic_and_batched():
     """Lists mode over a batch holding a periodic Taylor-Green box and a walled box."""
     import workloads as W
