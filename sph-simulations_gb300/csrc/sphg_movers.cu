@@ -35,9 +35,13 @@ namespace sphg {
 namespace {
 
 constexpr int kMergeThreads = 128;
-constexpr int kMergeSlots = 4;                               // slots per thread
+#ifndef SPHG_MERGE_SLOTS
+#define SPHG_MERGE_SLOTS 4
+#endif
+constexpr int kMergeSlots = SPHG_MERGE_SLOTS;               // slots per thread
 constexpr int kBlockSlots = kMergeThreads * kMergeSlots;    // 512 slots, 16 mask words
 constexpr int kSpanCap = 256;                               // movers inside a block's key span kept in shared memory
+static_assert(kBlockSlots / 32 <= kMergeThreads, "one thread per mask word of the block");
 
 // Slot `from` of the integrated state (its values p, v, id) to sorted position `to`.
 __device__ __forceinline__ void place_values(const MoverArgs& a, int64_t from, int64_t to, uint32_t key, float2 p,

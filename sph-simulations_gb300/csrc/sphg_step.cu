@@ -77,12 +77,13 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- reorder + cell ranges
-// kReorderSlots consecutive slots per thread: their keys in one 16-byte load,
-// the neighbouring keys of the first and last from the adjacent lanes.
+// kReorderSlots slots per thread, strided by the block size (coalesced), their
+// keys loaded before any is used.
 constexpr int kReorderSlots = 4;
 
 __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint32_t k, uint32_t kprev,
                                              uint32_t knext, bool gather, uint32_t ep) {
+  a.keyA[i] = k;
   if (gather) {  // after a full sort (a merge scattered the state already)
     const uint32_t src = a.perm[i];
     a.posA[i] = a.posB[src];
@@ -109,36 +110,24 @@ __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint3
 }
 
 __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
-  const int64_t base = ((int64_t)blockIdx.x * kThreads + threadIdx.x) * kReorderSlots;
-  const int lane = threadIdx.x & 31;
-  const bool whole = base + kReorderSlots <= a.n;  // keys buffers are 256-byte aligned: base is 16-byte aligned
-  uint32_t k[kReorderSlots];
-  if (whole) {
-    const uint4 v = *reinterpret_cast<const uint4*>(a.keyS + base);
-    k[0] = v.x; k[1] = v.y; k[2] = v.z; k[3] = v.w;
-  } else {
-#pragma unroll
-    for (int u = 0; u < kReorderSlots; ++u) k[u] = base + u < a.n ? a.keyS[base + u] : kNoIndex;
-  }
-  uint32_t kp = __shfl_up_sync(0xffffffffu, k[kReorderSlots - 1], 1);
-  uint32_t kn = __shfl_down_sync(0xffffffffu, k[0], 1);
-  if (lane == 0) kp = (base > 0 && base - 1 < a.n) ? a.keyS[base - 1] : kNoIndex;
-  if (lane == 31) kn = base + kReorderSlots < a.n ? a.keyS[base + kReorderSlots] : kNoIndex;
-  if (base >= a.n) return;
-  const bool gather = !(a.merged && *a.merged);
-  const uint32_t ep = *a.epoch;
-  if (whole) {
-    *reinterpret_cast<uint4*>(a.keyA + base) = make_uint4(k[0], k[1], k[2], k[3]);
-  } else {
-#pragma unroll
-    for (int u = 0; u < kReorderSlots; ++u)
-      if (base + u < a.n) a.keyA[base + u] = k[u];
-  }
+  const int64_t base = (int64_t)blockIdx.x * (kThreads * kReorderSlots) + threadIdx.x;
+  uint32_t k[kReorderSlots], kp[kReorderSlots], kn[kReorderSlots];
 #pragma unroll
   for (int u = 0; u < kReorderSlots; ++u) {
-    const int64_t i = base + u;
-    if (i < a.n)
-      reorder_slot(a, i, k[u], u ? k[u - 1] : kp, u + 1 < kReorderSlots ? k[u + 1] : kn, gather, ep);
+    const int64_t i = base + (int64_t)u * kThreads;
+    k[u] = kp[u] = kn[u] = kNoIndex;
+    if (i < a.n) {
+      k[u] = a.keyS[i];
+      kp[u] = i > 0 ? a.keyS[i - 1] : kNoIndex;
+      kn[u] = i + 1 < a.n ? a.keyS[i + 1] : kNoIndex;
+    }
+  }
+  const bool gather = !(a.merged && *a.merged);
+  const uint32_t ep = *a.epoch;
+#pragma unroll
+  for (int u = 0; u < kReorderSlots; ++u) {
+    const int64_t i = base + (int64_t)u * kThreads;
+    if (i < a.n) reorder_slot(a, i, k[u], kp[u], kn[u], gather, ep);
   }
 }
 
