@@ -519,7 +519,7 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     s->ddesc = A.take<InstDesc>(ninst);
     s->dbegins = A.take<int32_t>(ninst);
     s->dinst_tab = A.take<int32_t>((N >> sphg::kInstTabShift) + 2);
-    s->posA = A.take<float2>(N);
+    s->posA = A.take<float2>(N + 1);  // one padding entry: the density walk prefetches one past its last candidate
     s->posB = A.take<float2>(N);
     s->velB = A.take<float2>(N);
     s->acc = A.take<float2>(N);

@@ -150,6 +150,19 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
   }
 }
 
+#ifndef SPHG_DENSITY_TRIM
+#define SPHG_DENSITY_TRIM 1
+#endif
+// 1: the split walk skips the particle itself by splitting its own cell, the
+// prefetch past the last candidate reads the padding entry of the positions,
+// and the record is unconditional (the step's density pass always records)
+constexpr bool kDensityTrim = SPHG_DENSITY_TRIM != 0;
+#ifndef SPHG_DENSITY_PREFETCH2
+#define SPHG_DENSITY_PREFETCH2 0
+#endif
+// 1: the walk loads candidate positions two ahead instead of one (needs the trim's padding)
+constexpr bool kDensityPrefetch2 = SPHG_DENSITY_PREFETCH2 != 0 && kDensityTrim;
+
 template <int PREC, bool BATCHED, bool CSR, int T = kThreads>
 __global__ void __launch_bounds__(T) step_density(StepArgs a) {
   cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
@@ -174,7 +187,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
       S.add(t * t * t);
     }
   } else {
-    __shared__ uint4 s_cells[9][T];  // per thread: its non-empty stencil cells
+    __shared__ uint4 s_cells[10][T];  // per thread: its non-empty stencil cells (own cell split at itself)
     uint32_t* __restrict__ nbr = a.nbr;
     const uint32_t slots = (uint32_t)a.nbr_slots;
     const size_t n = (size_t)a.n;
@@ -187,7 +200,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
         ++cnt;
       }
     };
-    if (n < ((size_t)1 << 27)) {
+    if (nbr && n < ((size_t)1 << 27)) {
       // One loop over the candidates of the non-empty stencil cells, cells in
       // the stencil order and j ascending within a cell.  A warp then runs about
       // max over its lanes of the candidate total instead of the sum over the
@@ -217,6 +230,16 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
           const uint32_t tag = (uint32_t)k | ((PREC == 0 && ((wrapmask >> k) & 1u)) ? 16u : 0u);
           const float shx = (PREC == 1) ? (c1 == 0 ? 0.f : (c1 > 0 ? d.cs_x : -d.cs_x)) : 0.f;
           const float shy = (PREC == 1) ? (c2 == 0 ? 0.f : (c2 > 0 ? d.cs_y : -d.cs_y)) : 0.f;
+          if (kDensityTrim && PREC == 1 && k == 4) {
+            // own cell without the particle itself (its term W(0) = 1 is added
+            // first): [start, i) and (i, end), whichever are not empty
+            const uint32_t self = (uint32_t)i;
+            if (self > r[k].x)
+              s_cells[nseg++][tid] = make_uint4((r[k].x << 5) | tag, (self << 5) | tag, 0u, 0u);
+            if (self + 1 < r[k].y)
+              s_cells[nseg++][tid] = make_uint4(((self + 1) << 5) | tag, (r[k].y << 5) | tag, 0u, 0u);
+            continue;
+          }
           s_cells[nseg][tid] = make_uint4((r[k].x << 5) | tag, (r[k].y << 5) | tag, __float_as_uint(shx),
                                           __float_as_uint(shy));
           ++nseg;
@@ -229,7 +252,68 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
       uint32_t* rp = record ? nbr + i : nullptr;  // next record slot: nbr[cnt * n + i]
       bool border = false;
       if (PREC == 1) S.add(1.0f);  // own term W(0) first (plain sums keep the walk's order)
-      if (nseg > 0) {  // always: the particle's own cell holds it
+      if (nseg > 0 && kDensityPrefetch2) {
+        // one candidate: its pair term and record
+        auto visit = [&](uint32_t jj, float shx, float shy, float2 pj) {
+          const uint32_t j = jj >> 5;
+          float dx = (pi.x - pj.x) - shx;
+          float dy = (pi.y - pj.y) - shy;
+          float r2;
+          bool in;
+          if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
+            in = wrapped_pair(d, pi, pj, dx, dy);
+            r2 = fmaf(dx, dx, dy * dy);
+          } else {
+            r2 = fmaf(dx, dx, dy * dy);
+            in = r2 < h2_lo;
+            border |= !in && r2 <= h2_hi;
+          }
+          // split: the walk never meets the particle itself; the step always records
+          const bool other = (kDensityTrim && PREC == 1) || j != self;
+          const float t = fmaf(-r2, inv_h2, 1.0f);
+          S.add_fast((PREC == 1 ? in && other : in) ? t * t * t : 0.0f);
+          const bool rec = in && other && (kDensityTrim || record);
+          if (rec && cnt < slots) {
+            *rp = jj;
+            rp += n;
+          }
+          cnt += rec ? 1u : 0u;
+        };
+        // positions loaded two candidates ahead: the candidate after (j, e)
+        // in the queue, false past the last one (j is then the end of the last
+        // cell, at most slot n -- the positions hold one entry more)
+        int q = 1;
+        auto advance = [&](uint32_t& j, uint32_t& e, float& sx, float& sy) -> bool {
+          j += 32u;
+          if (j != e) return true;
+          if (q == nseg) return false;
+          const uint4 w = s_cells[q][tid];
+          ++q;
+          j = w.x;
+          e = w.y;
+          sx = __uint_as_float(w.z);
+          sy = __uint_as_float(w.w);
+          return true;
+        };
+        const uint4 w0 = s_cells[0][tid];
+        uint32_t jj = w0.x;
+        float shx = __uint_as_float(w0.z), shy = __uint_as_float(w0.w);
+        float2 pj = __ldg(pos + (jj >> 5));
+        uint32_t j1 = jj, e1 = w0.y;
+        float sx1 = shx, sy1 = shy;
+        bool m1 = advance(j1, e1, sx1, sy1);
+        float2 p1 = __ldg(pos + (j1 >> 5));
+        while (true) {
+          uint32_t j2 = j1, e2 = e1;
+          float sx2 = sx1, sy2 = sy1;
+          const bool m2 = m1 && advance(j2, e2, sx2, sy2);
+          const float2 p2 = __ldg(pos + (j2 >> 5));
+          visit(jj, shx, shy, pj);
+          if (!m1) break;
+          jj = j1; shx = sx1; shy = sy1; pj = p1;
+          j1 = j2; e1 = e2; sx1 = sx2; sy1 = sy2; p1 = p2; m1 = m2;
+        }
+      } else if (nseg > 0) {  // plain: always (the particle's own cell holds it); split: any other particle near
         uint4 w = s_cells[0][tid];
         int q = 1;
         uint32_t jj = w.x, je = w.y;
@@ -251,7 +335,9 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
               shyn = __uint_as_float(w.w);
             }
           }
-          const float2 pn = __ldg(pos + ((more ? jn : jj) >> 5));  // one candidate ahead
+          // one candidate ahead (past the last one: the end of its cell, at most
+          // slot n -- the positions hold one entry more)
+          const float2 pn = __ldg(pos + ((kDensityTrim || more ? jn : jj) >> 5));
           const uint32_t j = jj >> 5;
           float dx = (pi.x - pj.x) - shx;
           float dy = (pi.y - pj.y) - shy;
@@ -265,10 +351,11 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
             in = r2 < h2_lo;
             border |= !in && r2 <= h2_hi;
           }
-          const bool other = j != self;
+          // split: the walk never meets the particle itself; the step always records
+          const bool other = (kDensityTrim && PREC == 1) || j != self;
           const float t = fmaf(-r2, inv_h2, 1.0f);
           S.add_fast((PREC == 1 ? in && other : in) ? t * t * t : 0.0f);
-          const bool rec = in && other && record;
+          const bool rec = in && other && (kDensityTrim || record);
           if (rec && cnt < slots) {
             *rp = jj;
             rp += n;
@@ -580,14 +667,22 @@ constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered t
 #ifndef SPHG_FORCE_TAIL
 #define SPHG_FORCE_TAIL 1
 #endif
+#ifndef SPHG_FORCE_KAHAN
+#define SPHG_FORCE_KAHAN 0
+#endif
+// split precision: the force sums compensated by Kahan's method (1) or by TwoSum (0)
+constexpr bool kForceKahan = SPHG_FORCE_KAHAN != 0;
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
 
-// 1,024 threads per SM (64 registers) for one instance; the batched variants
+// 1,024 threads per SM (64 registers) for one instance (SPHG_FORCE_THREADS_PER_SM); the batched variants
 // are left to the compiler (their instance lookup needs more registers).
 template <int PREC, bool BATCHED, int MODE, bool CSR, int T = kThreads>
-__global__ void __launch_bounds__(T, BATCHED ? 0 : 1024 / T) step_force(StepArgs a) {
+#ifndef SPHG_FORCE_THREADS_PER_SM
+#define SPHG_FORCE_THREADS_PER_SM 1024
+#endif
+__global__ void __launch_bounds__(T, BATCHED ? 0 : SPHG_FORCE_THREADS_PER_SM / T) step_force(StepArgs a) {
   // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
   // recorded neighbours: one shared-memory load per pair instead of decoding k
   __shared__ float2 unit[16];
@@ -629,7 +724,7 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   const float4 vi = a.velpA[i];
-  typedef typename std::conditional<PREC == 1, CSum, PSum>::type Sum;
+  typedef typename std::conditional<PREC == 1, typename std::conditional<kForceKahan, KSum, CSum>::type, PSum>::type Sum;
   // one (compensated) sum per axis of every pair's pressure + viscosity (+ alpha) term
   Sum fx, fy;
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
