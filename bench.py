@@ -59,9 +59,10 @@ METRIC = ("particle-steps/s on 1 GB300, batched vs plain GPU path at ≤1e-5 rel
 UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, perm, rho) + sweep B 36 B
 # DRAM bytes per particle-step measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
-# summed over one merge-path iteration's kernels, caches flushed before each captured
-# launch; profiles/traffic_*.md)
-TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 104.9}
+# summed over one merge-path iteration's kernels -- re-sort merge, reorder, density, force --
+# caches flushed before each captured launch; profiles/traffic_dam_break_1m.md,
+# profiles/launches_batch_256.md)
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 104.0, "batch_256": 186.5}
 L2_FLUSH_BYTES = 256 << 20
 E2E_TRIALS = 3
 DATA = "synthetic: seeded jittered-lattice initial states (no dataset)"

@@ -139,21 +139,6 @@ struct CSum {
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
-// Kahan's compensated summation: c carries the negative of the rounding error
-// of the running sum, fed back into the next term (four additions a term
-// against TwoSum's six; error bound 2u |sum| + O(n u^2) sum |t|).
-struct KSum {
-  float s, c;
-  __device__ __forceinline__ KSum() : s(0.f), c(0.f) {}
-  __device__ __forceinline__ void add(float t) {
-    const float y = __fsub_rn(t, c);
-    const float sn = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(sn, s), y);
-    s = sn;
-  }
-  __device__ __forceinline__ float value() const { return __fsub_rn(s, c); }
-};
-
 struct PSum {
   float s;
   __device__ __forceinline__ PSum() : s(0.f) {}

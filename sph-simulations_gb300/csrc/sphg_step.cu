@@ -157,11 +157,7 @@ __device__ __forceinline__ void entry_vec(const InstDesc& d, float2 pi, float2 p
 // prefetch past the last candidate reads the padding entry of the positions,
 // and the record is unconditional (the step's density pass always records)
 constexpr bool kDensityTrim = SPHG_DENSITY_TRIM != 0;
-#ifndef SPHG_DENSITY_PREFETCH2
-#define SPHG_DENSITY_PREFETCH2 0
-#endif
-// 1: the walk loads candidate positions two ahead instead of one (needs the trim's padding)
-constexpr bool kDensityPrefetch2 = SPHG_DENSITY_PREFETCH2 != 0 && kDensityTrim;
+
 
 template <int PREC, bool BATCHED, bool CSR, int T = kThreads>
 __global__ void __launch_bounds__(T) step_density(StepArgs a) {
@@ -252,68 +248,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
       uint32_t* rp = record ? nbr + i : nullptr;  // next record slot: nbr[cnt * n + i]
       bool border = false;
       if (PREC == 1) S.add(1.0f);  // own term W(0) first (plain sums keep the walk's order)
-      if (nseg > 0 && kDensityPrefetch2) {
-        // one candidate: its pair term and record
-        auto visit = [&](uint32_t jj, float shx, float shy, float2 pj) {
-          const uint32_t j = jj >> 5;
-          float dx = (pi.x - pj.x) - shx;
-          float dy = (pi.y - pj.y) - shy;
-          float r2;
-          bool in;
-          if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
-            in = wrapped_pair(d, pi, pj, dx, dy);
-            r2 = fmaf(dx, dx, dy * dy);
-          } else {
-            r2 = fmaf(dx, dx, dy * dy);
-            in = r2 < h2_lo;
-            border |= !in && r2 <= h2_hi;
-          }
-          // split: the walk never meets the particle itself; the step always records
-          const bool other = (kDensityTrim && PREC == 1) || j != self;
-          const float t = fmaf(-r2, inv_h2, 1.0f);
-          S.add_fast((PREC == 1 ? in && other : in) ? t * t * t : 0.0f);
-          const bool rec = in && other && (kDensityTrim || record);
-          if (rec && cnt < slots) {
-            *rp = jj;
-            rp += n;
-          }
-          cnt += rec ? 1u : 0u;
-        };
-        // positions loaded two candidates ahead: the candidate after (j, e)
-        // in the queue, false past the last one (j is then the end of the last
-        // cell, at most slot n -- the positions hold one entry more)
-        int q = 1;
-        auto advance = [&](uint32_t& j, uint32_t& e, float& sx, float& sy) -> bool {
-          j += 32u;
-          if (j != e) return true;
-          if (q == nseg) return false;
-          const uint4 w = s_cells[q][tid];
-          ++q;
-          j = w.x;
-          e = w.y;
-          sx = __uint_as_float(w.z);
-          sy = __uint_as_float(w.w);
-          return true;
-        };
-        const uint4 w0 = s_cells[0][tid];
-        uint32_t jj = w0.x;
-        float shx = __uint_as_float(w0.z), shy = __uint_as_float(w0.w);
-        float2 pj = __ldg(pos + (jj >> 5));
-        uint32_t j1 = jj, e1 = w0.y;
-        float sx1 = shx, sy1 = shy;
-        bool m1 = advance(j1, e1, sx1, sy1);
-        float2 p1 = __ldg(pos + (j1 >> 5));
-        while (true) {
-          uint32_t j2 = j1, e2 = e1;
-          float sx2 = sx1, sy2 = sy1;
-          const bool m2 = m1 && advance(j2, e2, sx2, sy2);
-          const float2 p2 = __ldg(pos + (j2 >> 5));
-          visit(jj, shx, shy, pj);
-          if (!m1) break;
-          jj = j1; shx = sx1; shy = sy1; pj = p1;
-          j1 = j2; e1 = e2; sx1 = sx2; sy1 = sy2; p1 = p2; m1 = m2;
-        }
-      } else if (nseg > 0) {  // plain: always (the particle's own cell holds it); split: any other particle near
+      if (nseg > 0) {  // plain: always (the particle's own cell holds it); split: any other particle near
         uint4 w = s_cells[0][tid];
         int q = 1;
         uint32_t jj = w.x, je = w.y;
@@ -667,11 +602,7 @@ constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered t
 #ifndef SPHG_FORCE_TAIL
 #define SPHG_FORCE_TAIL 1
 #endif
-#ifndef SPHG_FORCE_KAHAN
-#define SPHG_FORCE_KAHAN 0
-#endif
-// split precision: the force sums compensated by Kahan's method (1) or by TwoSum (0)
-constexpr bool kForceKahan = SPHG_FORCE_KAHAN != 0;
+
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
@@ -724,7 +655,7 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   const float4 vi = a.velpA[i];
-  typedef typename std::conditional<PREC == 1, typename std::conditional<kForceKahan, KSum, CSum>::type, PSum>::type Sum;
+  typedef typename std::conditional<PREC == 1, CSum, PSum>::type Sum;
   // one (compensated) sum per axis of every pair's pressure + viscosity (+ alpha) term
   Sum fx, fy;
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
