@@ -602,6 +602,10 @@ constexpr int kForceBatch = SPHG_FORCE_BATCH;  // recorded neighbours gathered t
 #ifndef SPHG_FORCE_TAIL
 #define SPHG_FORCE_TAIL 1
 #endif
+#ifndef SPHG_SKIP_ZERO_VISCOSITY
+#define SPHG_SKIP_ZERO_VISCOSITY 1
+#endif
+constexpr bool kSkipZeroViscosity = SPHG_SKIP_ZERO_VISCOSITY != 0;
 
 
 template <int PREC, bool BATCHED, int MODE, bool CSR>
@@ -667,10 +671,14 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
     const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
     const float r = r2 * rinv;
     const float hr = h - r;
-    // viscosity (Laplacian): mu m / (rho_j pi h^6) 45 (h - r) (v_j - v_i)
-    const float vm = kv * vj.w * hr;
-    float tx = vm * (vj.x - vi.x);
-    float ty = vm * (vj.y - vi.y);
+    // viscosity (Laplacian): mu m / (rho_j pi h^6) 45 (h - r) (v_j - v_i); skipped when MU = 0 (the dam
+    // breaks' artificial viscosity replaces it), a branch uniform over the instance
+    float tx = 0.f, ty = 0.f;
+    if (!kSkipZeroViscosity || kv != 0.f) {
+      const float vm = kv * vj.w * hr;
+      tx = vm * (vj.x - vi.x);
+      ty = vm * (vj.y - vi.y);
+    }
     if (r2 > tol2) {
       // pressure (spiky gradient, symmetric p / rho^2 form)
       float s = kp * (vi.z + vj.z);
