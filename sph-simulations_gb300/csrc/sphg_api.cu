@@ -264,8 +264,7 @@ sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev, bo
   const StepArgs a = s->args();
   const int prec = s->opt.precision;
   if (s->tile_bits) SPHG_CUDA(cudaMemsetAsync(s->flags + 1, 0, sizeof(uint32_t), st));
-  // the mover count of this iteration's force pass (the re-sort has read the last one)
-  if (s->movers_on) SPHG_CUDA(cudaMemsetAsync(s->flags + 7, 0, sizeof(uint32_t), st));
+  // (the reorder zeroes the mover count of this iteration's force pass)
   SPHG_CUDA(sphg::launch_reorder(a, st));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[3], st));
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {

@@ -110,6 +110,9 @@ __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint3
 }
 
 __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
+  // the mover count of this iteration's force pass starts at zero (this
+  // iteration's re-sort, the kernel before, has read the last one)
+  if (a.mover_count && blockIdx.x == 0 && threadIdx.x == 0) *a.mover_count = 0;
   const int64_t base = (int64_t)blockIdx.x * (kThreads * kReorderSlots) + threadIdx.x;
   uint32_t k[kReorderSlots], kp[kReorderSlots], kn[kReorderSlots];
 #pragma unroll
