@@ -898,7 +898,13 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
   const int inst = blockIdx.y;
   const InstDesc& d = (a.ninst == 1) ? a.d0 : a.desc[inst];
   const int64_t cnt = d.end - d.begin;
-  const int64_t per = (cnt + chunks - 1) / chunks;
+  // chunks of this instance: with several instances about 1,024 particles a
+  // block (the grid's width is the largest instance's count; the blocks past an
+  // instance's own count leave at once, so a small instance of a mixed batch
+  // is not spread over thousands of nearly empty blocks)
+  const int ck = a.ninst == 1 ? chunks : (int)min((int64_t)chunks, max((int64_t)1, (cnt + 1023) / 1024));
+  if ((int)blockIdx.x >= ck) return;
+  const int64_t per = (cnt + ck - 1) / ck;
   const int64_t b = d.begin + per * blockIdx.x;
   const int64_t e = min((int64_t)d.end, b + per);
   // the instance constants used per particle, in registers
@@ -982,13 +988,13 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
   if (threadIdx.x == 0) {
     parts[blockIdx.x] = v;
     __threadfence();
-    last = atomicAdd(tickets + inst, 1u) == (uint32_t)chunks - 1u;
+    last = atomicAdd(tickets + inst, 1u) == (uint32_t)ck - 1u;
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
   DiagPart f = {};
-  for (int c = threadIdx.x; c < chunks; c += blockDim.x) part_add(f, load_part(parts + c));
+  for (int c = threadIdx.x; c < ck; c += blockDim.x) part_add(f, load_part(parts + c));
   f = part_block_reduce(f, sh);
   if (threadIdx.x != 0) return;
   tickets[inst] = 0;

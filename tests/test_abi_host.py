@@ -65,6 +65,10 @@ def test_host_argument_checks_fail_before_any_device_work(built):
     assert L.sphg_create(ctypes.byref(p), ctypes.byref(o), 10, ctypes.byref(h)) == S.INVALID_ARG
     o = S.options(tile_bits=4)  # tiles need Morton order; the default params are rowmajor
     assert L.sphg_create(ctypes.byref(p), ctypes.byref(o), 10, ctypes.byref(h)) == S.INVALID_ARG
+    # launch shapes the autotuner may pick: threads per block 64/128/256, one or two particles per density thread
+    for bad in (dict(block_threads=96), dict(block_threads=512), dict(cell_pairs=2), dict(cell_pairs=-1)):
+        o = S.options(**bad)
+        assert L.sphg_create(ctypes.byref(p), ctypes.byref(o), 10, ctypes.byref(h)) == S.INVALID_ARG, bad
     # the sorts keep 30-bit running counts in their look-back words
     sort = L.sphg_sort_pairs
     sort.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]
