@@ -535,6 +535,9 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     s->diag_out = A.take<double>((size_t)ninst * 6);
     s->hslot = A.take<sphg::HeaderSlot>(1);
     s->diag_tickets = A.take<uint32_t>(ninst);
+    // (instance, chunk) of every diagnostics block of several instances: at most
+    // one per 1,024 particles plus one per instance
+    s->ddiag_tab = A.take<uint32_t>(N / 1024 + (size_t)ninst + 1);
     if (s->opt.track_ids) {
       s->idsA = A.take<int32_t>(N);
       s->idsB = A.take<int32_t>(N);
@@ -604,14 +607,27 @@ sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int
     while (k + 1 < ninst && s->hbegins[k + 1] <= slot) ++k;
     s->hinst_tab[b] = (int32_t)k;
   }
+  // step headers of several instances: one diagnostics block per (instance,
+  // chunk) the instance uses (about 1,024 particles a block), as one 1-D grid
+  s->hdiag_tab.clear();
+  if (ninst > 1) {
+    const int chunks = sphg::diag_chunks(L.max_n, ninst, s->diag_chunks);
+    for (int k = 0; k < ninst; ++k)
+      for (int c = 0, ck = sphg::diag_instance_chunks(s->hdesc[k].end - s->hdesc[k].begin, chunks); c < ck; ++c)
+        s->hdiag_tab.push_back(((uint32_t)k << 12) | (uint32_t)c);
+  }
+  const size_t ntab = s->hdiag_tab.size();
   if (stream) {
     SPHG_CUDA(cudaMemcpyAsync(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice, *stream));
     SPHG_CUDA(cudaMemcpyAsync(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice, *stream));
     SPHG_CUDA(cudaMemcpyAsync(s->dinst_tab, s->hinst_tab.data(), sizeof(int32_t) * blocks, cudaMemcpyHostToDevice, *stream));
+    if (ntab)
+      SPHG_CUDA(cudaMemcpyAsync(s->ddiag_tab, s->hdiag_tab.data(), sizeof(uint32_t) * ntab, cudaMemcpyHostToDevice, *stream));
   } else {
     SPHG_CUDA(cudaMemcpy(s->ddesc, s->hdesc.data(), sizeof(InstDesc) * ninst, cudaMemcpyHostToDevice));
     SPHG_CUDA(cudaMemcpy(s->dbegins, s->hbegins.data(), sizeof(int32_t) * ninst, cudaMemcpyHostToDevice));
     SPHG_CUDA(cudaMemcpy(s->dinst_tab, s->hinst_tab.data(), sizeof(int32_t) * blocks, cudaMemcpyHostToDevice));
+    if (ntab) SPHG_CUDA(cudaMemcpy(s->ddiag_tab, s->hdiag_tab.data(), sizeof(uint32_t) * ntab, cudaMemcpyHostToDevice));
   }
   return SPHG_OK;
 }

@@ -41,6 +41,7 @@ struct sphg_sim {
   std::vector<InstDesc> hdesc;
   std::vector<int32_t> hbegins;
   std::vector<int32_t> hinst_tab;
+  std::vector<uint32_t> hdiag_tab;  // several instances: (instance << 12 | chunk) of each diagnostics block
   uint64_t total_keys = 0;
   int key_bits = 1;
   int diag_chunks = 1;
@@ -49,6 +50,7 @@ struct sphg_sim {
   InstDesc* ddesc = nullptr;
   int32_t* dbegins = nullptr;
   int32_t* dinst_tab = nullptr;  // instance of the first slot of each 256-slot block
+  uint32_t* ddiag_tab = nullptr;
   float2 *posA = nullptr, *posB = nullptr, *velB = nullptr, *acc = nullptr;
   float4* velpA = nullptr;
   float* rho = nullptr;
@@ -108,6 +110,8 @@ struct sphg_sim {
     a.desc = ddesc;
     a.begins = dbegins;
     a.inst_tab = dinst_tab;
+    a.diag_tab = hdiag_tab.empty() ? nullptr : ddiag_tab;
+    a.diag_blocks = (int)hdiag_tab.size();
     a.posA = posA;
     a.velpA = velpA;
     a.rho = rho;

@@ -895,17 +895,21 @@ __device__ __forceinline__ DiagPart load_part(const DiagPart* p) {
 template <int PREC, bool SLOT>
 __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks, double* partials,
                                                           uint32_t* tickets, double* out, HeaderSlot* slot) {
-  const int inst = blockIdx.y;
+  // block -> (instance, chunk): one instance: the grid's x; several: the
+  // layout's table (about 1,024 particles a block for every instance, so a
+  // small instance of a mixed batch is not spread over as many blocks as the
+  // largest one)
+  int inst = 0, chunk = blockIdx.x;
+  if (a.diag_tab) {
+    const uint32_t t = __ldg(a.diag_tab + blockIdx.x);
+    inst = (int)(t >> 12);
+    chunk = (int)(t & 4095u);
+  }
   const InstDesc& d = (a.ninst == 1) ? a.d0 : a.desc[inst];
   const int64_t cnt = d.end - d.begin;
-  // chunks of this instance: with several instances about 1,024 particles a
-  // block (the grid's width is the largest instance's count; the blocks past an
-  // instance's own count leave at once, so a small instance of a mixed batch
-  // is not spread over thousands of nearly empty blocks)
-  const int ck = a.ninst == 1 ? chunks : (int)min((int64_t)chunks, max((int64_t)1, (cnt + 1023) / 1024));
-  if ((int)blockIdx.x >= ck) return;
+  const int ck = a.diag_tab ? diag_instance_chunks(cnt, chunks) : chunks;
   const int64_t per = (cnt + ck - 1) / ck;
-  const int64_t b = d.begin + per * blockIdx.x;
+  const int64_t b = d.begin + per * chunk;
   const int64_t e = min((int64_t)d.end, b + per);
   // the instance constants used per particle, in registers
   const float lo_x = d.lo_x, hi_x = d.hi_x, lo_y = d.lo_y, hi_y = d.hi_y;
@@ -986,7 +990,7 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
   v = part_block_reduce(v, sh);
   DiagPart* parts = reinterpret_cast<DiagPart*>(partials) + (size_t)inst * chunks;
   if (threadIdx.x == 0) {
-    parts[blockIdx.x] = v;
+    parts[chunk] = v;
     __threadfence();
     last = atomicAdd(tickets + inst, 1u) == (uint32_t)ck - 1u;
   }
@@ -1006,9 +1010,9 @@ __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks
     return;
   }
   const size_t k = *(volatile uint32_t*)&slot->k;
-  for (int q = 0; q < 6; ++q) slot->out[(k * gridDim.y + inst) * 6 + q] = r[q];
+  for (int q = 0; q < 6; ++q) slot->out[(k * a.ninst + inst) * 6 + q] = r[q];
   __threadfence();
-  if (atomicAdd(&slot->done, 1u) == gridDim.y - 1) {
+  if (atomicAdd(&slot->done, 1u) == (uint32_t)a.ninst - 1u) {
     slot->done = 0;
     slot->k += 1;
     __threadfence();
@@ -1206,7 +1210,7 @@ int diag_chunks(int64_t max_inst_n, int ninst, int cap) {
 
 cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partials, uint32_t* tickets, int chunks,
                                double* out, cudaStream_t s) {
-  dim3 g(chunks, a.ninst);
+  const dim3 g = a.diag_tab ? dim3(a.diag_blocks) : dim3(chunks, a.ninst);
   if (precision) step_diag<1, false><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, out, nullptr);
   else step_diag<0, false><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, out, nullptr);
   return cudaGetLastError();
@@ -1214,7 +1218,7 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
 
 cudaError_t launch_diagnostics_slot(const StepArgs& a, int precision, double* partials, uint32_t* tickets,
                                     int chunks, HeaderSlot* slot, cudaStream_t s) {
-  dim3 g(chunks, a.ninst);
+  const dim3 g = a.diag_tab ? dim3(a.diag_blocks) : dim3(chunks, a.ninst);
   if (precision) step_diag<1, true><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, nullptr, slot);
   else step_diag<0, true><<<g, kDiagThreads, 0, s>>>(a, chunks, partials, tickets, nullptr, slot);
   return cudaGetLastError();

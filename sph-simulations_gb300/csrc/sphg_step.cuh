@@ -23,6 +23,8 @@ struct StepArgs {
   const InstDesc* desc;        // [ninst]
   const int32_t* begins;       // [ninst]
   const int32_t* inst_tab;     // [n >> kInstTabShift + 1] instance of the first slot of each block
+  const uint32_t* diag_tab;    // several instances: instance << 12 | chunk of each diagnostics block (or null)
+  int diag_blocks;             // entries of diag_tab
   // sorted ("current") state
   float2* posA;
   float4* velpA;               // (vx, vy, p/rho^2, 1/rho)
@@ -96,6 +98,12 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
 // Diagnostics chunks of the largest instance (at most cap; the partial buffer
 // holds ninst x chunks x 6 doubles).
 int diag_chunks(int64_t max_inst_n, int ninst, int cap = 4096);
+// Diagnostics blocks of one instance of `count` particles among several
+// (about 1,024 particles a block, at most `chunks`).
+__host__ __device__ inline int diag_instance_chunks(int64_t count, int chunks) {
+  const int64_t c = (count + 1023) / 1024;
+  return (int)(c < 1 ? 1 : (c > chunks ? chunks : c));
+}
 // out[6*inst + {0, 1}] = max |v|^2, max |a|^2 of each instance (a.acc must hold the forces).
 cudaError_t launch_cfl(const StepArgs& a, double* partials, int chunks, double* out, cudaStream_t s);
 // CSR neighbour lists of the current state (sphg_lists.cu); returns an sphg_status.
