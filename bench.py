@@ -19,6 +19,8 @@ iteration with the launch configuration the autotuner picks.
                    written into pinned host memory, final download
   config_run       all the configuration's iterations (1,000) timed as one
                    run, with the share that re-sorted by merging
+  dam_break_12k,   nested records of the 12,800-particle dam break (plain FP32)
+  tgv_262k         and of the periodic 512 x 512 Taylor-Green vortex
   dam_break_1m     nested record of the 1,000,000-particle dam break (1000 x
                    1000 particles, dx = 0.0005, split precision): device time,
                    roofline, re-sort mix of the timed steps and of its whole
@@ -519,6 +521,12 @@ def run_gpu(args):
             r1m, _ = device_record("dam_break_1m", args, sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1),
                                    stream, args.steps, args.warmup, with_e2e=False)
             nested["dam_break_1m"] = r1m
+        # the 12,800-particle dam break (plain FP32) and the periodic 512 x 512 Taylor-Green vortex
+        for extra_name in ("dam_break_12k", "tgv_262k"):
+            if extra_name != name:
+                rx, _ = device_record(extra_name, args, sphg.options(precision=sphg.PLAIN, track_ids=0, use_graph=1),
+                                      stream, args.steps, args.warmup, with_e2e=False)
+                nested[extra_name] = rx
         # the lists compute mode (CSR neighbour lists assembled every iteration) on the same dam break
         rl, _ = device_record("dam_break_1m", args,
                               sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1, compute="lists"),

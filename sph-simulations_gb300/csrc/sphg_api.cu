@@ -536,8 +536,8 @@ sphg_status alloc_arena(sphg_sim* s, size_t N, uint64_t keys, int ninst, int dia
     s->hslot = A.take<sphg::HeaderSlot>(1);
     s->diag_tickets = A.take<uint32_t>(ninst);
     // (instance, chunk) of every diagnostics block of several instances: at most
-    // one per 1,024 particles plus one per instance
-    s->ddiag_tab = A.take<uint32_t>(N / 1024 + (size_t)ninst + 1);
+    // one per 4,096 particles plus one per instance
+    s->ddiag_tab = A.take<uint32_t>(N / 4096 + (size_t)ninst + 1);
     if (s->opt.track_ids) {
       s->idsA = A.take<int32_t>(N);
       s->idsB = A.take<int32_t>(N);
@@ -608,7 +608,7 @@ sphg_status apply_layout(sphg_sim* s, int ninst, const sphg_params* p, const int
     s->hinst_tab[b] = (int32_t)k;
   }
   // step headers of several instances: one diagnostics block per (instance,
-  // chunk) the instance uses (about 1,024 particles a block), as one 1-D grid
+  // chunk) the instance uses (about 4,096 particles a block), as one 1-D grid
   s->hdiag_tab.clear();
   if (ninst > 1) {
     const int chunks = sphg::diag_chunks(L.max_n, ninst, s->diag_chunks);

@@ -896,7 +896,7 @@ template <int PREC, bool SLOT>
 __global__ void __launch_bounds__(kDiagThreads) step_diag(StepArgs a, int chunks, double* partials,
                                                           uint32_t* tickets, double* out, HeaderSlot* slot) {
   // block -> (instance, chunk): one instance: the grid's x; several: the
-  // layout's table (about 1,024 particles a block for every instance, so a
+  // layout's table (about 4,096 particles a block for every instance, so a
   // small instance of a mixed batch is not spread over as many blocks as the
   // largest one)
   int inst = 0, chunk = blockIdx.x;
@@ -1189,7 +1189,7 @@ cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_
 int diag_chunks(int64_t max_inst_n, int ninst, int cap) {
   int64_t c;
   if (ninst > 1) {
-    c = (max_inst_n + 1023) / 1024;  // about four particles per thread
+    c = (max_inst_n + 4095) / 4096;  // about 16 particles per thread (diag_instance_chunks)
   } else {
     // one instance: two blocks per SM, all resident at once and equally loaded
     static const int sms = [] {

@@ -99,9 +99,9 @@ cudaError_t launch_diagnostics(const StepArgs& a, int precision, double* partial
 // holds ninst x chunks x 6 doubles).
 int diag_chunks(int64_t max_inst_n, int ninst, int cap = 4096);
 // Diagnostics blocks of one instance of `count` particles among several
-// (about 1,024 particles a block, at most `chunks`).
+// (about 4,096 particles a block -- 16 a thread --, at most `chunks`).
 __host__ __device__ inline int diag_instance_chunks(int64_t count, int chunks) {
-  const int64_t c = (count + 1023) / 1024;
+  const int64_t c = (count + 4095) / 4096;
   return (int)(c < 1 ? 1 : (c > chunks ? chunks : c));
 }
 // out[6*inst + {0, 1}] = max |v|^2, max |a|^2 of each instance (a.acc must hold the forces).
