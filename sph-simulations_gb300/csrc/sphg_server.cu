@@ -806,7 +806,11 @@ sphg_status sphg_server_result(sphg_server* s, int64_t id, double* x, double* y,
   auto it = s->reqs.find(id);
   if (it == s->reqs.end()) return fail(SPHG_INVALID_ARG, "unknown request id");
   SrvReq& r = it->second;
-  if (r.state < 2) return fail(SPHG_NOT_READY, "request not finished");
+  if (r.state < 2) {
+    // a serving thread that stopped on an error will not finish it
+    if (s->worker_status != SPHG_OK) return fail(s->worker_status, "serving loop stopped: " + s->worker_error);
+    return fail(SPHG_NOT_READY, "request not finished");
+  }
   if (r.state == 2) {
     if (s->running.load()) {
       poll_retiring(s);
