@@ -115,6 +115,12 @@ typedef struct sphg_options {
   int32_t cell_pairs;  /* density pass: 0 (default) one particle per thread; 1 one thread
                           carries two particles of a cell (they share the stencil walk;
                           the same results) */
+  int32_t fused;       /* 1: each iteration that merges is ONE cooperative launch (re-sort,
+                          cell ranges, density, forces as phases between grid-wide
+                          barriers) instead of four kernels -- for small and medium
+                          workloads, whose kernel boundaries cost as much as their work;
+                          the same results.  Sorted compute mode without cell tiles only;
+                          0 (default): a graph of four kernels */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;

@@ -225,7 +225,7 @@ namespace sphg_detail {
 // The incremental re-sort's kernels (see sphg_movers.cu).  cond, when not 0,
 // is the graph's conditional handle that guards the full sort: the decision
 // kernel sets it to 0 when the merge handled the iteration.
-sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond) {
+static sphg::MoverArgs mover_args(sphg_sim* s, unsigned long long cond) {
   sphg::MoverArgs m;
   m.n = s->n;
   m.keyA = s->keyA;
@@ -244,7 +244,27 @@ sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond
   m.posA = s->posA;
   m.velpA = s->velpA;
   m.idsA = s->opt.track_ids ? s->idsA : nullptr;
-  SPHG_CUDA(sphg::launch_movers(m, st));
+  return m;
+}
+
+sphg_status enqueue_movers(sphg_sim* s, cudaStream_t st, unsigned long long cond) {
+  SPHG_CUDA(sphg::launch_movers(mover_args(s, cond), st));
+  return SPHG_OK;
+}
+
+// The iteration as one cooperative launch (sphg_options.fused): available for
+// the sorted compute mode with the merge re-sort and no cell tiles.
+bool fused_on(sphg_sim* s) {
+  if (s->opt.fused != 1 || !s->movers_on || s->tile_bits || s->opt.compute != SPHG_COMPUTE_SORTED || !s->nbr ||
+      s->n == 0)
+    return false;
+  return sphg::fused_blocks(s->args(), s->opt.precision) > 0;
+}
+
+// post: after a full sort (ranges, density, forces); else the merge first.
+sphg_status enqueue_fused(sphg_sim* s, cudaStream_t st, bool post, unsigned long long cond) {
+  SPHG_CUDA(sphg::launch_fused(s->args(), mover_args(s, cond), s->opt.precision, s->flags + 10, s->flags + 12, post,
+                               st));
   return SPHG_OK;
 }
 
@@ -316,6 +336,18 @@ sphg_status enqueue_after_sort(sphg_sim* s, cudaStream_t st, cudaEvent_t* ev, bo
 // With ev (6 events) the phase boundaries are recorded: start, keys, sort,
 // reorder, density, force.
 sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first, cudaEvent_t* ev) {
+  if (!ev && fused_on(s)) {
+    // one launch when the merge handles the iteration; else the full sort and
+    // the launch's post part (the full sort's kernels and the post launch
+    // return at once on the merge's decision word)
+    if (first) SPHG_CUDA(sphg::launch_keys(s->args(), s->opt.precision, st));
+    const bool inc = !first && !s->force_full_sort;
+    s->force_full_sort = false;
+    if (inc) SPHG_TRY(enqueue_fused(s, st, false, 0));
+    else SPHG_CUDA(cudaMemsetAsync(s->flags + 3, 0, sizeof(uint32_t), st));
+    SPHG_TRY(enqueue_full_sort(s, st, inc ? s->flags + 3 : nullptr));
+    return enqueue_fused(s, st, true, 0);
+  }
   if (ev) SPHG_CUDA(cudaEventRecord(ev[0], st));
   if (first) SPHG_CUDA(sphg::launch_keys(s->args(), s->opt.precision, st));
   if (ev) SPHG_CUDA(cudaEventRecord(ev[1], st));
@@ -368,7 +400,9 @@ sphg_status build_graph_conditional(sphg_sim* s, cudaGraphExec_t* exec, bool hea
   if (cudaStreamBeginCaptureToGraph(s->cap_stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
       cudaSuccess)
     return done(fail(SPHG_CUDA_ERROR, "capture to graph"));
-  sphg_status st = enqueue_movers(s, s->cap_stream, (unsigned long long)h);
+  const bool fused = fused_on(s);
+  sphg_status st = fused ? enqueue_fused(s, s->cap_stream, false, (unsigned long long)h)
+                         : enqueue_movers(s, s->cap_stream, (unsigned long long)h);
   if (st != SPHG_OK) return done(st);
   cudaStreamCaptureStatus cst;
   const cudaGraphNode_t* deps = nullptr;
@@ -388,13 +422,14 @@ sphg_status build_graph_conditional(sphg_sim* s, cudaGraphExec_t* exec, bool hea
       cudaSuccess)
     return done(fail(SPHG_CUDA_ERROR, "capture of the conditional body"));
   st = enqueue_full_sort(s, s->cap_stream2, nullptr);
+  if (st == SPHG_OK && fused) st = enqueue_fused(s, s->cap_stream2, true, 0);  // ranges, density, forces
   cudaGraph_t body_out = nullptr;
   const cudaError_t eb = cudaStreamEndCapture(s->cap_stream2, &body_out);
   if (st != SPHG_OK) return done(st);
   if (eb != cudaSuccess) return done(fail(SPHG_CUDA_ERROR, "end of the conditional body capture"));
   if (cudaStreamUpdateCaptureDependencies(s->cap_stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
     return done(fail(SPHG_CUDA_ERROR, "capture dependencies"));
-  st = enqueue_after_sort(s, s->cap_stream, nullptr);
+  if (!fused) st = enqueue_after_sort(s, s->cap_stream, nullptr);
   if (st == SPHG_OK && header) st = enqueue_header(s, s->cap_stream);
   if (st != SPHG_OK) return done(st);
   cudaGraph_t out = nullptr;
@@ -468,6 +503,7 @@ sphg_status check_options(sphg_sim* s, int ninst, const sphg_params* p) {
   if (bt != 0 && bt != 64 && bt != 128 && bt != 256)
     return fail(SPHG_INVALID_ARG, "block_threads must be 0 (default), 64, 128 or 256");
   if (s->opt.cell_pairs < 0 || s->opt.cell_pairs > 1) return fail(SPHG_INVALID_ARG, "cell_pairs must be 0 or 1");
+  if (s->opt.fused < 0 || s->opt.fused > 1) return fail(SPHG_INVALID_ARG, "fused must be 0 or 1");
   if (s->opt.compute == SPHG_COMPUTE_LISTS) {
     if (tb > 0) return fail(SPHG_INVALID_ARG, "the lists compute mode runs without cell tiles");
     tb = -1;
@@ -681,6 +717,7 @@ void sphg_default_options(sphg_options* o) {
   o->resort = 1;
   o->block_threads = 0;
   o->cell_pairs = 0;
+  o->fused = 0;
 }
 
 const char* sphg_last_error_string(void) { return g_err.c_str(); }
@@ -850,11 +887,13 @@ sphg_status sphg_step(sphg_sim* s, int64_t nsteps, void* stream) {
 // look-back (a wait that gave up) and the incremental re-sort's consistency
 // word.  Read at the synchronising calls; both stay set.
 static sphg_status device_errors(sphg_sim* s, cudaStream_t st) {
-  uint32_t w[3] = {0, 0, 0};
+  uint32_t w[4] = {0, 0, 0, 0};
   SPHG_CUDA(cudaMemcpyAsync(&w[0], sphg::sort_error_word(s->scratch), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaMemcpyAsync(&w[1], s->flags + 5, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaMemcpyAsync(&w[2], s->flags + 8, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  SPHG_CUDA(cudaMemcpyAsync(&w[3], s->flags + 12, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SPHG_CUDA(cudaStreamSynchronize(st));
+  if (w[3]) return fail(SPHG_TIMEOUT, "a grid-wide barrier of the single-launch iteration gave up; the state is not valid");
   if (w[0]) return fail(SPHG_TIMEOUT, "a radix-sort look-back wait gave up; the state is not valid");
   if (w[1]) return fail(SPHG_CUDA_ERROR, "inconsistent incremental re-sort record; the state is not valid");
   if (w[2]) return fail(SPHG_CAPACITY, "lists mode: the neighbour lists outgrew their buffer (twice the pre-loop's "
@@ -1075,7 +1114,8 @@ sphg_status sphg_get_debug(sphg_sim* s, int32_t which, void* host, void* stream)
         SPHG_CUDA(cudaMemcpyAsync(c, s->flags + 3, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         SPHG_CUDA(cudaStreamSynchronize(st));
       }
-      c[2] = (uint32_t)((s->key_bits + 7) / 8 + 1);  // histogram + radix passes of a full sort
+      // histogram + radix passes of a full sort (+ the post part of the single-launch iteration)
+      c[2] = (uint32_t)((s->key_bits + 7) / 8 + 1 + (fused_on(s) ? 1 : 0));
       std::memcpy(host, c, sizeof(c));
       return SPHG_OK;
     }
@@ -1251,6 +1291,10 @@ int32_t sphg_launches_per_step(const sphg_sim* s) {
   // reorder + density + force (+ the three incremental re-sort kernels; + list
   // count, three scan kernels and list fill in the lists mode).  An iteration
   // that merges launches (key_bits + 7) / 8 + 1 kernels fewer in a graph.
+  // With the single-launch iteration: the launch (which only decides), the
+  // histogram + radix passes and the launch's post part; an iteration that
+  // merges is the one launch.
+  if (fused_on(const_cast<sphg_sim*>(s))) return passes + 3;
   return passes + 4 + (s->movers_on ? 1 : 0) + (s->opt.compute == SPHG_COMPUTE_LISTS ? 5 : 0);
 }
 

@@ -188,6 +188,9 @@ void demorton_host(uint32_t z, int& x, int& y);
 // first: the iteration after an upload (cell keys computed; in lists mode the
 // index buffer is sized from this iteration's list total, a host synchronisation).
 sphg_status enqueue_step(sphg_sim* s, cudaStream_t st, bool first = false, cudaEvent_t* ev = nullptr);
+// The single-launch iteration applies (sphg_options.fused, sorted mode, merge
+// re-sort, no tiles, and the device can launch it cooperatively).
+bool fused_on(sphg_sim* s);
 // Captures (once per layout) the CUDA graph of one iteration (header: followed
 // by its step header into the header slot).
 sphg_status build_graph(sphg_sim* s, bool header = false);

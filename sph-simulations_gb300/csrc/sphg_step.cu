@@ -28,12 +28,22 @@
 #include <cuda_runtime.h>
 
 #include "sphg_movers.cuh"
+#include "sphg_movers_body.cuh"
 #include "sphg_neighbor.cuh"
 #include "sphg_step.cuh"
 
 namespace sphg {
 
 constexpr int kThreads = 128;  // 128-thread blocks: measured a little faster than 256 and 512 for the passes
+
+// Stores of the phase outputs that a later phase of the fused single-launch
+// iteration (step_fused) reads: there they bypass L1 (st.global.cg), so no
+// SM keeps a partial line of data other SMs write in the same launch.
+template <bool FUSED, class V>
+__device__ __forceinline__ void st_out(V* p, V v) {
+  if constexpr (FUSED) __stcg(p, v);
+  else *p = v;
+}
 
 // ---------------------------------------------------------------- keys
 template <int PREC, bool BATCHED>
@@ -81,22 +91,23 @@ __global__ void __launch_bounds__(kThreads) step_keys(StepArgs a) {
 // keys loaded before any is used.
 constexpr int kReorderSlots = 4;
 
+template <bool FUSED>
 __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint32_t k, uint32_t kprev,
                                              uint32_t knext, bool gather, uint32_t ep) {
-  a.keyA[i] = k;
+  st_out<FUSED>(a.keyA + i, k);
   if (gather) {  // after a full sort (a merge scattered the state already)
     const uint32_t src = a.perm[i];
-    a.posA[i] = a.posB[src];
+    st_out<FUSED>(a.posA + i, a.posB[src]);
     const float2 v = a.velB[src];
-    a.velpA[i] = make_float4(v.x, v.y, 0.f, 0.f);
-    if (a.track_ids) a.idsA[i] = a.idsB[src];
+    st_out<FUSED>(a.velpA + i, make_float4(v.x, v.y, 0.f, 0.f));
+    if (a.track_ids) st_out<FUSED>(a.idsA + i, a.idsB[src]);
   }
   uint32_t* r = reinterpret_cast<uint32_t*>(a.ranges);
   if (k != kprev) {
-    r[4 * (size_t)k] = (uint32_t)i;
-    r[4 * (size_t)k + 2] = ep;
+    st_out<FUSED>(r + 4 * (size_t)k, (uint32_t)i);
+    st_out<FUSED>(r + 4 * (size_t)k + 2, ep);
   }
-  if (k != knext) r[4 * (size_t)k + 1] = (uint32_t)(i + 1);
+  if (k != knext) st_out<FUSED>(r + 4 * (size_t)k + 1, (uint32_t)(i + 1));
   if (a.tile_bits) {
     const int sh = 2 * a.tile_bits;
     const uint32_t t = k >> sh;
@@ -109,11 +120,10 @@ __device__ __forceinline__ void reorder_slot(const StepArgs& a, int64_t i, uint3
   }
 }
 
-__global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
-  // the mover count of this iteration's force pass starts at zero (this
-  // iteration's re-sort, the kernel before, has read the last one)
-  if (a.mover_count && blockIdx.x == 0 && threadIdx.x == 0) *a.mover_count = 0;
-  const int64_t base = (int64_t)blockIdx.x * (kThreads * kReorderSlots) + threadIdx.x;
+// Reorder block blk: slots [blk * 512, blk * 512 + 512).
+template <bool FUSED>
+__device__ __forceinline__ void reorder_block(const StepArgs& a, int64_t blk) {
+  const int64_t base = blk * (kThreads * kReorderSlots) + threadIdx.x;
   uint32_t k[kReorderSlots], kp[kReorderSlots], kn[kReorderSlots];
 #pragma unroll
   for (int u = 0; u < kReorderSlots; ++u) {
@@ -130,8 +140,15 @@ __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
 #pragma unroll
   for (int u = 0; u < kReorderSlots; ++u) {
     const int64_t i = base + (int64_t)u * kThreads;
-    if (i < a.n) reorder_slot(a, i, k[u], kp[u], kn[u], gather, ep);
+    if (i < a.n) reorder_slot<FUSED>(a, i, k[u], kp[u], kn[u], gather, ep);
   }
+}
+
+__global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
+  // the mover count of this iteration's force pass starts at zero (this
+  // iteration's re-sort, the kernel before, has read the last one)
+  if (a.mover_count && blockIdx.x == 0 && threadIdx.x == 0) *a.mover_count = 0;
+  reorder_block<false>(a, blockIdx.x);
 }
 
 // ---------------------------------------------------------------- density + pressure
@@ -163,10 +180,11 @@ constexpr bool kDensityTrim = SPHG_DENSITY_TRIM != 0;
 
 
 template <int PREC, bool BATCHED, bool CSR, int T = kThreads>
-__global__ void __launch_bounds__(T) step_density(StepArgs a) {
-  cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+__global__ void __launch_bounds__(T) step_density(StepArgs a);
+
+// Density + pressure of particle i (i < n); FUSED: the outputs bypass L1 (st_out).
+template <int PREC, bool BATCHED, bool CSR, int T, bool FUSED>
+__device__ __forceinline__ void density_particle(const StepArgs& a, int64_t i) {
   typename std::conditional<BATCHED, const InstDesc&, const InstDesc>::type d = inst_ref<BATCHED>(a, i);
   if (BATCHED && !d.active) return;  // a finished served instance
   const uint32_t key = a.keyA[i];
@@ -195,7 +213,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
       const float t = fmaf(-r2, inv_h2, 1.0f);
       S.add(t * t * t);
       if (nbr && (e >> 5) != (uint32_t)i) {  // record the pair for the force pass
-        if (cnt < slots) nbr[cnt * n + i] = e;
+        if (cnt < slots) st_out<FUSED>(nbr + cnt * n + i, e);
         ++cnt;
       }
     };
@@ -295,7 +313,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
           S.add_fast((PREC == 1 ? in && other : in) ? t * t * t : 0.0f);
           const bool rec = in && other && (kDensityTrim || record);
           if (rec && cnt < slots) {
-            *rp = jj;
+            st_out<FUSED>(rp, jj);
             rp += n;
           }
           cnt += rec ? 1u : 0u;
@@ -329,7 +347,7 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
         accept((j << 5) | tag, r2);
       });
     }
-    if (nbr) a.ncount[i] = cnt;
+    if (nbr) st_out<FUSED>(a.ncount + i, cnt);
   }
   float rho, drho;
   if constexpr (PREC == 1) {
@@ -341,8 +359,16 @@ __global__ void __launch_bounds__(T) step_density(StepArgs a) {
   }
   const float inv = 1.0f / rho;
   const float P = d.k * drho * inv * inv;
-  a.rho[i] = rho;
-  reinterpret_cast<float2*>(a.velpA + i)[1] = make_float2(P, inv);
+  st_out<FUSED>(a.rho + i, rho);
+  st_out<FUSED>(reinterpret_cast<float2*>(a.velpA + i) + 1, make_float2(P, inv));
+}
+
+template <int PREC, bool BATCHED, bool CSR, int T>
+__global__ void __launch_bounds__(T) step_density(StepArgs a) {
+  cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  density_particle<PREC, BATCHED, CSR, T, false>(a, i);
 }
 
 // ---------------------------------------------------------------- density, two particles of a cell per thread
@@ -616,10 +642,14 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
 
 // 1,024 threads per SM (64 registers) for one instance (SPHG_FORCE_THREADS_PER_SM); the batched variants
 // are left to the compiler (their instance lookup needs more registers).
-template <int PREC, bool BATCHED, int MODE, bool CSR, int T = kThreads>
 #ifndef SPHG_FORCE_THREADS_PER_SM
 #define SPHG_FORCE_THREADS_PER_SM 1024
 #endif
+template <int PREC, bool BATCHED, int MODE, bool CSR>
+__device__ __forceinline__ void force_slot(const StepArgs& a, int64_t i, const float2* unit);
+
+template <int PREC, bool BATCHED, int MODE, bool CSR, int T = kThreads>
+
 __global__ void __launch_bounds__(T, BATCHED ? 0 : SPHG_FORCE_THREADS_PER_SM / T) step_force(StepArgs a) {
   // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
   // recorded neighbours: one shared-memory load per pair instead of decoding k
@@ -630,7 +660,13 @@ __global__ void __launch_bounds__(T, BATCHED ? 0 : SPHG_FORCE_THREADS_PER_SM / T
   }
   __syncthreads();
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  force_slot<PREC, BATCHED, MODE, CSR>(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, unit);
+}
+
+// Force pass of slot i (every thread of a warp calls it, i may be >= n): the
+// forces and, in integrate mode, the update, the new key and the mover record.
+template <int PREC, bool BATCHED, int MODE, bool CSR>
+__device__ __forceinline__ void force_slot(const StepArgs& a, int64_t i, const float2* unit) {
   // slots of a finished served instance are skipped (no pair, no integration, no mover bit)
   const bool valid = i < a.n && (!BATCHED || inst_ref<BATCHED>(a, i).active);
   const bool track = MODE == kForceIntegrate && a.mover_mask != nullptr;
@@ -779,6 +815,80 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
     return 0;
   }
   return integrate_and_key<PREC>(a, d, i, cx, cy, pi, vi, ax, ay);
+}
+
+// ---------------------------------------------------------------- the iteration in one launch
+// step_fused runs re-sort (merge) -> cell ranges -> density -> forces +
+// integration as four phases of ONE cooperative launch, separated by grid-wide
+// barriers, instead of four kernels: for small and medium workloads the
+// kernel boundaries cost as much as the work.  Every phase is the same device
+// code as its stand-alone kernel (the same bits), over the blocks in a
+// grid-stride loop.  Data a phase writes and a later phase of the same launch
+// reads is stored past L1 (st.global.cg) and the merge reads the keys and cell
+// ranges the reorder will rewrite past L1 (ld.global.cg): no SM holds a stale
+// line of them.  When more than kMoverCap slots changed, the launch only
+// records that (merge_decide) and the full radix sort runs, followed by the
+// launch in "post" mode (ranges, density, forces).
+constexpr int kBarrierSpinLimit = 1 << 22;  // about a quarter second of 64 ns sleeps
+
+// Grid-wide barrier of a cooperative launch: bar[0] counts arrivals, bar[1] is
+// the generation the last arrival advances.  Bounded: a wait that gives up
+// sets *err (reported as SPHG_TIMEOUT) and lets the block go on.
+__device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t gen = atomicAdd(bar + 1, 0u);
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      int spins = 0;
+      while (*(volatile uint32_t*)(bar + 1) == gen) {
+        if (++spins > kBarrierSpinLimit) {
+          atomicExch(err, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <int PREC, bool BATCHED>
+__global__ void __launch_bounds__(kThreads, BATCHED ? 6 : 8) step_fused(StepArgs a, MoverArgs m, uint32_t* bar, uint32_t* err,
+                                                          int post) {
+  __shared__ float2 unit[16];
+  if (threadIdx.x < 16) {
+    const int k = threadIdx.x;
+    unit[k] = k < 9 ? make_float2((float)(k / 3 - 1), (float)(k % 3 - 1)) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int64_t G = gridDim.x;
+  if (!post) {
+    uint32_t movers = 0;
+    if (!merge_decide(m, blockIdx.x == 0 && threadIdx.x == 0, &movers)) return;  // the full sort runs instead
+    const int64_t nb = (a.n + kMergeBlockSlots - 1) / kMergeBlockSlots;
+    for (int64_t b = blockIdx.x; b < nb; b += G) merge_block<true>(m, b, (uint32_t)nb, movers);
+    grid_barrier(bar, err);
+  } else if (a.merged && *(volatile const uint32_t*)a.merged) {
+    return;  // stream-launched iteration that merged: nothing left for the post launch
+  }
+  if (a.mover_count && blockIdx.x == 0 && threadIdx.x == 0) atomicExch(a.mover_count, 0u);
+  const int64_t nr = (a.n + kThreads * kReorderSlots - 1) / (kThreads * kReorderSlots);
+  for (int64_t b = blockIdx.x; b < nr; b += G) reorder_block<true>(a, b);
+  grid_barrier(bar, err);
+  const int64_t np = (a.n + kThreads - 1) / kThreads;
+  for (int64_t b = blockIdx.x; b < np; b += G) {
+    const int64_t i = b * kThreads + threadIdx.x;
+    if (i < a.n) density_particle<PREC, BATCHED, false, kThreads, true>(a, i);
+  }
+  grid_barrier(bar, err);
+  for (int64_t b = blockIdx.x; b < np; b += G)
+    force_slot<PREC, BATCHED, kForceIntegrate, false>(a, b * kThreads + threadIdx.x, unit);
 }
 
 // ---------------------------------------------------------------- diagnostics
@@ -1235,6 +1345,54 @@ cudaError_t launch_cell_keys_plain(const InstDesc& d, const float* x, const floa
                                    int32_t* keys, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   cell_keys_plain<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, x, y, n, keys);
+  return cudaGetLastError();
+}
+
+// Co-resident blocks of step_fused (0: it cannot be launched cooperatively).
+template <int PREC, bool BATCHED>
+static int fused_max_blocks() {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, step_fused<PREC, BATCHED>, kThreads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return cached = 0;
+  }
+  return cached = per * sms;
+}
+
+int fused_blocks(const StepArgs& a, int precision) {
+  const bool b = (a.ninst > 1 || a.force_batched);
+  const int mx = precision ? (b ? fused_max_blocks<1, true>() : fused_max_blocks<1, false>())
+                           : (b ? fused_max_blocks<0, true>() : fused_max_blocks<0, false>());
+  const int64_t need = (a.n + kThreads - 1) / kThreads;
+  return (int)std::min<int64_t>(mx, std::max<int64_t>(need, 1));
+}
+
+cudaError_t launch_fused(const StepArgs& a, const MoverArgs& m, int precision, uint32_t* bar, uint32_t* err, bool post,
+                         cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const int g = fused_blocks(a, precision);
+  if (g <= 0) return cudaErrorNotSupported;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const bool b = (a.ninst > 1 || a.force_batched);
+  const int p = post ? 1 : 0;
+  cudaError_t e;
+  if (precision) e = b ? cudaLaunchKernelEx(&cfg, step_fused<1, true>, a, m, bar, err, p)
+                       : cudaLaunchKernelEx(&cfg, step_fused<1, false>, a, m, bar, err, p);
+  else e = b ? cudaLaunchKernelEx(&cfg, step_fused<0, true>, a, m, bar, err, p)
+             : cudaLaunchKernelEx(&cfg, step_fused<0, false>, a, m, bar, err, p);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

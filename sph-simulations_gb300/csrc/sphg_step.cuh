@@ -65,6 +65,15 @@ struct StepArgs {
 enum ForceMode { kForceIntegrate = 0, kForceOnly = 1 };
 
 cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s);
+// The iteration in one cooperative launch (merge -> ranges -> density -> forces;
+// post: after a full sort, ranges -> density -> forces).  bar: two zeroed words,
+// err: set when a grid barrier's wait gave up.  cudaErrorNotSupported when the
+// device cannot launch it cooperatively.
+struct MoverArgs;
+cudaError_t launch_fused(const StepArgs& a, const MoverArgs& m, int precision, uint32_t* bar, uint32_t* err,
+                         bool post, cudaStream_t s);
+// Blocks of the fused launch for this handle (0: not available).
+int fused_blocks(const StepArgs& a, int precision);
 cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_density(const StepArgs& a, int precision, cudaStream_t s, bool csr = false);
 cudaError_t launch_force(const StepArgs& a, int precision, int mode, cudaStream_t s, bool csr = false);

@@ -58,7 +58,8 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("track_ids", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
                 ("compute", ctypes.c_int32), ("resort", ctypes.c_int32),
-                ("block_threads", ctypes.c_int32), ("cell_pairs", ctypes.c_int32)]
+                ("block_threads", ctypes.c_int32), ("cell_pairs", ctypes.c_int32),
+                ("fused", ctypes.c_int32)]
 
 
 _lib = None
@@ -168,7 +169,7 @@ def params(**kw):
 
 
 def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None, resort=None,
-            block_threads=None, cell_pairs=None):
+            block_threads=None, cell_pairs=None, fused=None):
     o = Options()
     lib().sphg_default_options(ctypes.byref(o))
     if resort is not None:
@@ -177,6 +178,8 @@ def options(precision=PLAIN, track_ids=1, use_graph=1, tile_bits=0, compute=None
         o.block_threads = int(block_threads)
     if cell_pairs is not None:
         o.cell_pairs = int(cell_pairs)
+    if fused is not None:
+        o.fused = int(fused)
     o.precision = precision
     o.track_ids = track_ids
     o.use_graph = use_graph

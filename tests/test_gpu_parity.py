@@ -684,7 +684,7 @@ def test_lists_mode_reports_lists_outgrowing_their_buffer():
 
 
 @pytest.mark.parametrize("opt", [dict(cell_pairs=1), dict(block_threads=64), dict(block_threads=256),
-                                 dict(cell_pairs=1, block_threads=64)])
+                                 dict(cell_pairs=1, block_threads=64), dict(fused=1), dict(fused=1, use_graph=0)])
 def test_launch_shapes_give_identical_results(opt):
     """The autotuner's launch shapes (threads per block, two particles of a cell
     per density thread) visit the same pairs in the same order: the same bits."""
@@ -695,12 +695,45 @@ def test_launch_shapes_give_identical_results(opt):
     cat = [np.concatenate([i[k] for i in inst]) for k in (1, 2, 3, 4)]
     out = []
     for o in ({}, opt):
-        b = S.Sim(prms, counts, S.options(precision=S.SPLIT, **o))
+        o = dict(o)
+        g = o.pop("use_graph", 1)
+        b = S.Sim(prms, counts, S.options(precision=S.SPLIT, use_graph=g, **o))
         b.upload(*cat)
         b.preloop()
         b.step(20)
         out.append(b.download())
         b.close()
+    for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
+        assert (out[0][f] == out[1][f]).all(), f
+
+
+@pytest.mark.parametrize("graph", [1, 0])
+@pytest.mark.parametrize("prec", ["plain", "split"])
+def test_single_launch_iteration_equals_kernel_graph(prec, graph):
+    """The iteration as one cooperative launch (merge, ranges, density, forces
+    between grid-wide barriers) gives the bits of the four-kernel iteration --
+    also on iterations where more than 8,192 particles change cell and the full
+    radix sort runs between the launch's decision and its post part."""
+    S = _sphg()
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    # ballistic particles (no pressure, viscosity or gravity: the forces are exactly zero) fast enough that
+    # about a third change cell every step
+    x, y, vx, vy = jittered(240, 200, 0.004, seed=31, vel=80.0)
+    kw = dict(order="morton", h=0.0052, dt=2e-5, lo=(0, 0), hi=(1.2, 1.0), k=0.0, mu=0.0, gx=0.0, gy=0.0, alpha=0.0)
+    out, resort = [], []
+    for fused in (0, 1):
+        sim = S.Sim(S.params(**kw), len(x), S.options(precision=P, fused=fused, use_graph=graph))
+        sim.upload(x, y, vx, vy)
+        sim.preloop()
+        merged = []
+        for _ in range(12):
+            sim.step(1)
+            merged.append(int(sim.debug(S.DBG_RESORT)[0]))
+        out.append(sim.download())
+        resort.append(merged)
+        sim.close()
+    assert resort[0] == resort[1]
+    assert 0 in resort[1], "the case must exercise the full sort"
     for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
         assert (out[0][f] == out[1][f]).all(), f
 

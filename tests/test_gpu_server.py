@@ -216,3 +216,29 @@ def test_compaction_keeps_every_result_bitwise():
     for k, rid in enumerate(ids):
         for f in ("x", "y", "vx", "vy", "rho", "ids"):
             assert (done[rid][f] == alone[k][f]).all(), (k, f)
+
+
+def test_served_results_equal_with_the_single_launch_iteration():
+    """A server whose iterations are single cooperative launches gives the same
+    bits as one running the four-kernel graph."""
+    import sphg as S
+    reqs = _requests(6, 8)
+    outs = []
+    for fused in (0, 1):
+        srv = S.Server(2e9, opts=S.options(fused=fused))
+        ids = [srv.submit(S.params(**r[0]), *r[1:5], r[5]) for r in reqs]
+        done = {}
+        for _ in range(5000):
+            srv.tick()
+            for rid in ids:
+                if rid not in done:
+                    r = srv.result(rid)
+                    if r is not None:
+                        done[rid] = r
+            if len(done) == len(ids):
+                break
+        srv.close()
+        outs.append([done[i] for i in ids])
+    for a, b in zip(*outs):
+        for f in ("x", "y", "vx", "vy", "rho", "ids"):
+            assert (a[f] == b[f]).all(), f
