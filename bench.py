@@ -292,9 +292,9 @@ def device_record(name, args, opts, stream, steps, warmup, with_e2e=True, world=
                                  base=opts, steps=5, stream=sptr)
         opts = best
         tuned = {"ms_per_step": ms, "tile_bits": best.tile_bits, "resort": best.resort,
-                 "block_threads": best.block_threads, "cell_pairs": best.cell_pairs,
+                 "block_threads": best.block_threads, "cell_pairs": best.cell_pairs, "fused": best.fused,
                  "searched": "tile_bits {off,3,4,5} x (untiled) re-sort {merge, full} x block {64,128,256} "
-                             "x particles per density thread {2 of a cell, 1}"}
+                             "x particles per density thread {2 of a cell, 1}; single cooperative launch per iteration"}
     sim = sphg.Sim(sprm, counts, opts)
     sim.upload(x, y, vx, vy, stream=sptr)
     sim.preloop(stream=sptr)
@@ -434,7 +434,7 @@ def plain_path(prm, counts, x, y, vx, vy, opts, stream, steps):
                    "stepped in turn on one stream; same options as the batched run"}
 
 
-def serve_record(seconds, rate, steps, budget_gb):
+def serve_record(seconds, rate, steps, budget_gb, fused=0):
     """Serving: Poisson arrivals of dam-break / Taylor-Green lattice requests
     submitted at their arrival times to a server whose loop runs on its own
     thread and stream; latency = result in host memory - submission."""
@@ -442,7 +442,7 @@ def serve_record(seconds, rate, steps, budget_gb):
     import sphg
     reqs = W.lattice_requests(rate=rate, seconds=seconds, seed=0, steps=steps)
     srv = sphg.Server(budget_gb * 1e9, max_instances=8192,
-                      opts=sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1))
+                      opts=sphg.options(precision=sphg.SPLIT, track_ids=0, use_graph=1, fused=fused))
     srv.start(torch.cuda.current_device())
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
@@ -480,6 +480,7 @@ def serve_record(seconds, rate, steps, budget_gb):
             "appends": int(st["appends"]), "compactions": int(st["compactions"]),
             "graph_builds": int(st["graph_builds"]),
             "config": {"workload": "serve", "rate_per_s": rate, "seconds": seconds, "steps_per_request": steps,
+                       "single_launch_iterations": bool(fused),
                        "hbm_budget_gb": budget_gb, "particles_range": [1000, 200000], "precision": "split",
                        "mix": "dam-break / Taylor-Green 50/50, states generated on the device at admission",
                        "capacity_particles": st["cap_particles"], "capacity_cell_keys": st["cap_keys"]},
@@ -501,7 +502,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     name = args.workload
     prec = sphg.SPLIT if WORKLOADS[name]["precision"] == "split" else sphg.PLAIN
-    opts = sphg.options(precision=prec, track_ids=0, use_graph=args.graph, compute=args.compute)
+    opts = sphg.options(precision=prec, track_ids=0, use_graph=args.graph, compute=args.compute, fused=args.fused)
     is_batch = WORKLOADS[name]["kind"] == "batch"
     rec, (w, prm, x, y, vx, vy) = device_record(name, args, opts, stream, args.steps, args.warmup,
                                                 world=world, tune=is_batch and args.graph == 1)
@@ -512,7 +513,7 @@ def run_gpu(args):
             t = rec["autotune"]
             tuned_opts = sphg.options(precision=prec, track_ids=0, use_graph=1, tile_bits=t["tile_bits"],
                                       resort=t["resort"], block_threads=t["block_threads"],
-                                      cell_pairs=t["cell_pairs"])
+                                      cell_pairs=t["cell_pairs"], fused=t["fused"])
         plain = plain_path(prm, w["counts"], x, y, vx, vy, tuned_opts, stream, max(3, min(args.steps, 20)))
         extra = {"plain_gpu_path": plain, "batched_vs_plain": rec["value"] / plain["value"]}
     nested = {}
@@ -533,7 +534,8 @@ def run_gpu(args):
                               stream, args.steps, args.warmup, with_e2e=False)
         nested["dam_break_1m_lists"] = rl
         if args.serve_seconds > 0:
-            nested["serve"] = serve_record(args.serve_seconds, args.rate, args.serve_steps, args.budget_gb)
+            nested["serve"] = serve_record(args.serve_seconds, args.rate, args.serve_steps, args.budget_gb,
+                                           args.serve_fused)
     if world > 1:
         torch.distributed.barrier()
     if rank == 0:
@@ -590,6 +592,8 @@ def main():
                     help="seconds of CPU baseline sampling (0 = skip)")
     ap.add_argument("--compute", default="sorted", choices=["sorted", "lists"],
                     help="compute mode of the named workload (lists: CSR neighbour lists every iteration)")
+    ap.add_argument("--fused", type=int, default=0,
+                    help="1: the named workload's iterations as single cooperative launches")
     ap.add_argument("--graph", type=int, default=1,
                     help="1: every iteration replays a CUDA graph; 0: stream-launched kernels (for profilers)")
     ap.add_argument("--no-nested", action="store_true",
@@ -598,6 +602,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve: arrival window (0 = skip)")
     ap.add_argument("--serve-steps", type=int, default=500, help="serve: steps per request")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
+    ap.add_argument("--serve-fused", type=int, default=0, help="serve: iterations as single cooperative launches")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -609,7 +614,7 @@ def main():
     elif args.workload == "serve":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        rec = serve_record(args.serve_seconds, args.rate, args.serve_steps, args.budget_gb)
+        rec = serve_record(args.serve_seconds, args.rate, args.serve_steps, args.budget_gb, args.serve_fused)
         line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.serve_steps,
                 "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic: seeded Poisson request stream of jittered lattices generated on the device"}

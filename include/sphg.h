@@ -120,7 +120,11 @@ typedef struct sphg_options {
                           barriers) instead of four kernels -- for small and medium
                           workloads, whose kernel boundaries cost as much as their work;
                           the same results.  Sorted compute mode without cell tiles only;
-                          0 (default): a graph of four kernels */
+                          its grid fills the GPU, so two handles must not run such
+                          iterations at the same time on one GPU (different streams):
+                          their barriers would wait on each other until their bounded
+                          waits give up (SPHG_TIMEOUT).  0 (default): a graph of four
+                          kernels */
 } sphg_options;
 
 typedef struct sphg_sim sphg_sim;

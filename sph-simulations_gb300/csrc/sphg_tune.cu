@@ -7,7 +7,7 @@
 // a cell sharing the stencil walk, or one), the threads per block of the
 // density and force passes (64, 128, 256) and the re-sort strategy
 // (incremental merge of the particles that changed cell, or the full radix
-// sort every iteration).  Each candidate gets its own handle with the caller's
+// sort every iteration); and the iteration as one cooperative launch.  Each candidate gets its own handle with the caller's
 // state, runs the pre-loop and a few warm-up iterations, then `steps` timed
 // iterations (CUDA events on the caller's stream).  Results are remembered per
 // workload signature (instance sizes, precision, orders), so a second call for
@@ -80,19 +80,21 @@ extern "C" sphg_status sphg_autotune(int32_t ninst, const sphg_params* p, const 
   Tuned win{b, -1.0};
   sphg_status res = SPHG_OK;
   struct Cand {
-    int tb, resort, block, pairs;
+    int tb, resort, block, pairs, fused;
   };
   std::vector<Cand> cands;
   for (int tb : tiles) {
     if (tb > 0) {  // the tile kernels do not record cell changes; their blocks are their own
-      cands.push_back({tb, 0, 0, 0});
+      cands.push_back({tb, 0, 0, 0, 0});
       continue;
     }
+    // the iteration as one cooperative launch (merge re-sort, 128 threads, one particle per thread)
+    if (b.compute == SPHG_COMPUTE_SORTED) cands.push_back({tb, 1, 128, 0, 1});
     for (int resort : {1, 0})
       for (int block : {128, 64, 256})
         for (int pairs : {0, 1}) {
           if (b.compute == SPHG_COMPUTE_LISTS && pairs) continue;  // lists mode: no stencil walk in the density
-          cands.push_back({tb, resort, block, pairs});
+          cands.push_back({tb, resort, block, pairs, 0});
         }
   }
   for (const Cand& cd : cands) {
@@ -102,6 +104,7 @@ extern "C" sphg_status sphg_autotune(int32_t ninst, const sphg_params* p, const 
       o.resort = cd.resort;
       o.block_threads = cd.block;
       o.cell_pairs = cd.pairs;
+      o.fused = cd.fused;
       sphg_sim* s = nullptr;
       sphg_status st2 = sphg_create_batch(ninst, p, counts, &o, &s);
       if (st2 == SPHG_OK) st2 = sphg_upload(s, x, y, vx, vy, stream);
