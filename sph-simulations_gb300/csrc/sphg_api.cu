@@ -1288,7 +1288,7 @@ int32_t sphg_launches_per_step(const sphg_sim* s) {
   if (!s || s->n == 0) return 0;
   const int passes = (s->key_bits + 7) / 8;
   // an iteration that runs the full sort: its histogram kernel + radix passes +
-  // reorder + density + force (+ the three incremental re-sort kernels; + list
+  // reorder + density + force (+ the incremental re-sort's merge kernel; + list
   // count, three scan kernels and list fill in the lists mode).  An iteration
   // that merges launches (key_bits + 7) / 8 + 1 kernels fewer in a graph.
   // With the single-launch iteration: the launch (which only decides), the

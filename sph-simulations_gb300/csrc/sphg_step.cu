@@ -640,17 +640,28 @@ constexpr bool kSkipZeroViscosity = SPHG_SKIP_ZERO_VISCOSITY != 0;
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, const float2* unit);
 
-// 1,024 threads per SM (64 registers) for one instance (SPHG_FORCE_THREADS_PER_SM); the batched variants
-// are left to the compiler (their instance lookup needs more registers).
+// Threads per SM the force pass is compiled for.  Split precision: 1,152
+// (nine 128-thread blocks, 56 registers) for one instance and 1,024 (eight
+// blocks, 64 registers; the instance lookup spills a few bytes) for the batched
+// variants -- measured on the GB300 against 1,024 / the compiler's own 72
+// registers: 29.8 against 31.7 us on the 1M dam break, 0.408 against 0.420 ms
+// per batch_256 iteration.  Plain positions need more registers: 1,024 for one
+// instance, the compiler's choice batched (fewer spill).
 #ifndef SPHG_FORCE_THREADS_PER_SM
-#define SPHG_FORCE_THREADS_PER_SM 1024
+#define SPHG_FORCE_THREADS_PER_SM 1152
 #endif
+#ifndef SPHG_FORCE_BATCHED_THREADS_PER_SM
+#define SPHG_FORCE_BATCHED_THREADS_PER_SM 1024
+#endif
+constexpr int force_threads_per_sm(int prec, bool batched) {
+  return prec == 1 ? (batched ? SPHG_FORCE_BATCHED_THREADS_PER_SM : SPHG_FORCE_THREADS_PER_SM) : (batched ? 0 : 1024);
+}
 template <int PREC, bool BATCHED, int MODE, bool CSR>
 __device__ __forceinline__ void force_slot(const StepArgs& a, int64_t i, const float2* unit);
 
 template <int PREC, bool BATCHED, int MODE, bool CSR, int T = kThreads>
 
-__global__ void __launch_bounds__(T, BATCHED ? 0 : SPHG_FORCE_THREADS_PER_SM / T) step_force(StepArgs a) {
+__global__ void __launch_bounds__(T, force_threads_per_sm(PREC, BATCHED) / T) step_force(StepArgs a) {
   // unit stencil offsets (c1, c2) of the tags k = 3 (c1 + 1) + (c2 + 1) of the
   // recorded neighbours: one shared-memory load per pair instead of decoding k
   __shared__ float2 unit[16];
