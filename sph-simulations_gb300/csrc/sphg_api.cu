@@ -154,6 +154,8 @@ sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64
   d.mass_d = p.mass;
   d.hi_xd = p.hi[0];
   d.hi_yd = p.hi[1];
+  d.inv_cs_xd = 1.0 / cs[0];
+  d.inv_cs_yd = 1.0 / cs[1];
   d.half_Lx_d = 0.5 * L[0];
   d.half_Ly_d = 0.5 * L[1];
   if (!std::isfinite(d.wd) || !std::isfinite(d.kp) || !std::isfinite(d.kv) || !std::isfinite(d.ka) ||
@@ -226,7 +228,7 @@ namespace sphg_detail {
 // is the graph's conditional handle that guards the full sort: the decision
 // kernel sets it to 0 when the merge handled the iteration.
 static sphg::MoverArgs mover_args(sphg_sim* s, unsigned long long cond) {
-  sphg::MoverArgs m;
+  sphg::MoverArgs m = {};
   m.n = s->n;
   m.keyA = s->keyA;
   m.mask = s->mmask;

@@ -46,6 +46,7 @@ struct __align__(16) InstDesc {
   double lo_xd, lo_yd, cs_xd, cs_yd, Lx_d, Ly_d, h2_d;
   double mass_d, hi_xd, hi_yd;
   double half_Lx_d, half_Ly_d;  // periodic minimum image
+  double inv_cs_xd, inv_cs_yd;  // 1 / cs (FP64): cell index of an FP64 position without a division
 };
 
 // ---------------------------------------------------------------- Morton codes

@@ -29,6 +29,7 @@ struct MoverArgs {
   float2* posA;
   float4* velpA;
   int32_t* idsA;
+  uint32_t mover_blocks;   // the stand-alone kernel's leading blocks that place the movers (set by launch_movers)
 };
 
 // One launch: the decision (merge when at most kMoverCap slots changed, else

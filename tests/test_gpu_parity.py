@@ -1065,6 +1065,64 @@ def test_particles_outside_the_high_walls(prec):
     sim.close()
 
 
+@pytest.mark.parametrize("prec", ["split", "plain"])
+def test_direct_host_access_vector_and_scalar_paths(prec):
+    """The device-side conversion of the caller's arrays reads and writes two
+    particles a thread with 16-byte accesses when every array is 16-byte
+    aligned, one a thread otherwise: both equal the pinned staging path bit for
+    bit, for an odd particle count (the last particle alone), and report the
+    first non-finite particle of a pair or of the odd tail."""
+    S = _sphg()
+    if not S.device_attributes(0)["pageable_access"]:
+        pytest.skip("the device cannot access pageable host memory")
+    import workloads as W
+    P = S.SPLIT if prec == "split" else S.PLAIN
+    prm, x, y, vx, vy = W.dam_break(13, 77, 0.01, seed=5)  # 1,001 particles
+    n = len(x)
+    assert n % 2 == 1
+    vx = np.linspace(-0.2, 0.3, n)
+    vy = np.linspace(0.1, -0.4, n)
+
+    def views(offset):
+        out = []
+        for a in (x, y, vx, vy):
+            buf = np.zeros(n + 2, np.float64)
+            buf[offset:offset + n] = a
+            out.append(buf[offset:offset + n])
+        return out
+
+    def out_views(offset):
+        d = {}
+        for k in ("x", "y", "vx", "vy", "rho", "fx", "fy"):
+            d[k] = np.zeros(n + 2, np.float64)[offset:offset + n]
+        d["ids"] = np.zeros(n + 2, np.int32)[offset:offset + n]
+        return d
+
+    results = []
+    for mode, offset in ((0, 0), (2, 0), (2, 1), (1, 0), (1, 1)):
+        arrs = views(offset)
+        assert (arrs[0].ctypes.data % 16 == 0) == (offset == 0)
+        sim = S.Sim(S.params(**prm), n, S.options(precision=P))
+        sim.set_host_access(mode)
+        sim.upload(*arrs)
+        sim.preloop()
+        sim.step(3)
+        results.append(sim.download(out=out_views(offset)))
+        for bad_at in (0, 5, n - 1):
+            bad = [a.copy() for a in arrs] if offset == 0 else views(offset)
+            bad[2][bad_at] = np.inf
+            if bad_at == 0:
+                bad[3][1] = np.nan  # both of the first pair: the first is reported
+            with pytest.raises(S.SphgError) as ei:
+                sim.upload(*bad)
+            assert ei.value.status == S.NONFINITE and ("particle %d" % bad_at) in str(ei.value), (mode, offset, bad_at)
+        sim.close()
+    ref = results[0]
+    for r in results[1:]:
+        for f in ("x", "y", "vx", "vy", "rho", "fx", "fy", "ids"):
+            assert np.array_equal(r[f], ref[f]), f
+
+
 @pytest.mark.parametrize("prec", ["plain", "split"])
 def test_direct_host_access_equals_staging(prec):
     """Upload/download converting the caller's arrays on the device (pageable host
