@@ -246,6 +246,7 @@ static sphg::MoverArgs mover_args(sphg_sim* s, unsigned long long cond) {
   m.posA = s->posA;
   m.velpA = s->velpA;
   m.idsA = s->opt.track_ids ? s->idsA : nullptr;
+  m.early_next = s->n <= sphg::kEarlyNextMaxN ? 1 : 0;
   return m;
 }
 

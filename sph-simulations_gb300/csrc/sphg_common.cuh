@@ -158,6 +158,18 @@ __device__ __forceinline__ int find_instance(const int32_t* __restrict__ begins,
   return lo;
 }
 
+// Lets the next kernel of the stream (launched with programmatic dependent
+// launch) be scheduled now: its blocks take the SMs this grid's last blocks
+// leave and wait in cudaGridDependencySynchronize() for this grid to finish
+// (which still orders every memory access).  Called at the start of the step
+// kernels when the state is small (a few waves a kernel: the tail and the next
+// launch are a large share of it), not for large ones, where it measured slower
+// (12,800 particles: 36.5 -> 34.4 us an iteration; 4.4M: 0.410 -> 0.419 ms).
+constexpr int64_t kEarlyNextMaxN = (int64_t)1 << 19;
+__device__ __forceinline__ void allow_next_kernel(int early) {
+  if (early) cudaTriggerProgrammaticLaunchCompletion();
+}
+
 // Launch with programmatic dependent launch: the kernel may be scheduled while
 // the previous kernel in the stream finishes; it must call
 // cudaGridDependencySynchronize() before touching that kernel's results (a

@@ -106,6 +106,7 @@ struct sphg_sim {
     a.n = n;
     a.ninst = ninst;
     a.track_ids = opt.track_ids;
+    a.early_next = n <= sphg::kEarlyNextMaxN ? 1 : 0;
     if (!hdesc.empty()) a.d0 = hdesc[0];
     a.desc = ddesc;
     a.begins = dbegins;

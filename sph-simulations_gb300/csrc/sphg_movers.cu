@@ -39,6 +39,7 @@ namespace {
 
 __global__ void __launch_bounds__(kMergeThreads) movers_merge(MoverArgs a) {
   cudaGridDependencySynchronize();  // the mover record of the previous force pass
+  allow_next_kernel(a.early_next);
   uint32_t m = 0;
   if (!merge_decide(a, blockIdx.x == 0 && threadIdx.x == 0, &m)) return;
   constexpr uint32_t W = kMergeThreads / 32;

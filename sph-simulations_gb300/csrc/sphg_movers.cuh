@@ -30,6 +30,7 @@ struct MoverArgs {
   float4* velpA;
   int32_t* idsA;
   uint32_t mover_blocks;   // the stand-alone kernel's leading blocks that place the movers (set by launch_movers)
+  int early_next;          // let the next kernel be scheduled at the start (allow_next_kernel)
 };
 
 // One launch: the decision (merge when at most kMoverCap slots changed, else

@@ -145,6 +145,8 @@ __device__ __forceinline__ void reorder_block(const StepArgs& a, int64_t blk) {
 }
 
 __global__ void __launch_bounds__(kThreads) step_reorder(StepArgs a) {
+  cudaGridDependencySynchronize();  // the sorted keys (and the decision word) of the re-sort
+  allow_next_kernel(a.early_next);
   // the mover count of this iteration's force pass starts at zero (this
   // iteration's re-sort, the kernel before, has read the last one)
   if (a.mover_count && blockIdx.x == 0 && threadIdx.x == 0) *a.mover_count = 0;
@@ -366,6 +368,7 @@ __device__ __forceinline__ void density_particle(const StepArgs& a, int64_t i) {
 template <int PREC, bool BATCHED, bool CSR, int T>
 __global__ void __launch_bounds__(T) step_density(StepArgs a) {
   cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
+  allow_next_kernel(a.early_next);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   density_particle<PREC, BATCHED, CSR, T, false>(a, i);
@@ -445,6 +448,7 @@ template <int PREC, bool BATCHED, int T = kThreads>
 __global__ void __launch_bounds__(T) step_density_pairs(StepArgs a) {
   constexpr int kPairSlots = 2 * T;
   cudaGridDependencySynchronize();  // the sorted state and cell ranges of the reorder
+  allow_next_kernel(a.early_next);
   __shared__ uint32_t s_key[kPairSlots];
   __shared__ uint16_t s_chunk[kPairSlots];  // offset of each pair's (or odd particle's) first slot | partner << 15
   __shared__ uint32_t s_wmax[T / 32], s_wcnt[T / 32];
@@ -671,6 +675,7 @@ __global__ void __launch_bounds__(T, force_threads_per_sm(PREC, BATCHED) / T) st
   }
   __syncthreads();
   cudaGridDependencySynchronize();  // densities, pressures and neighbour lists of the density pass
+  allow_next_kernel(a.early_next);
   force_slot<PREC, BATCHED, MODE, CSR>(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, unit);
 }
 
@@ -1234,7 +1239,8 @@ cudaError_t launch_keys(const StepArgs& a, int precision, cudaStream_t s) {
 
 cudaError_t launch_reorder(const StepArgs& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
-  step_reorder<<<blocks_for(a.n, kThreads * kReorderSlots), kThreads, 0, s>>>(a);
+  cudaError_t e = launch_pdl(step_reorder, dim3(blocks_for(a.n, kThreads * kReorderSlots)), dim3(kThreads), 0, s, a);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -16,6 +16,7 @@ struct StepArgs {
   int64_t n;
   int ninst;
   int track_ids;
+  int early_next;              // let the next kernel be scheduled at this kernel's start (allow_next_kernel)
   int force_batched;           // 1: per-instance descriptor kernels even for one instance
   int block;                   // threads per block of the density and force passes (64, 128, 256)
   int cell_pairs;              // 1: the density pass carries two particles of a cell per thread
