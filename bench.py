@@ -64,7 +64,7 @@ BYTES_PER_PARTICLE_STEP = 80.0  # algorithmic: sweep A 44 B (state in/out, key, 
 # summed over one merge-path iteration's kernels -- re-sort merge, reorder, density, force --
 # caches flushed before each captured launch; profiles/traffic_dam_break_1m.md,
 # profiles/launches_batch_256.md)
-TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 104.3, "batch_256": 186.5}
+TRAFFIC_PER_PARTICLE_STEP = {"dam_break_1m": 104.3, "batch_256": 186.3}
 L2_FLUSH_BYTES = 256 << 20
 E2E_TRIALS = 3
 DATA = "synthetic: seeded jittered-lattice initial states (no dataset)"
