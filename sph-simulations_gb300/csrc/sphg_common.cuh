@@ -140,6 +140,35 @@ struct CSum {
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
+// Paired FP32 arithmetic (one sm_100-family instruction for both components;
+// each component rounds exactly as the scalar _rn operation does).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// CSum of both axes at once: the same TwoSum per component in paired
+// instructions (the same bits as two CSum).
+struct CSum2 {
+  float2 s, c;
+  __device__ __forceinline__ CSum2() : s(make_float2(0.f, 0.f)), c(make_float2(0.f, 0.f)) {}
+  __device__ __forceinline__ void add(float2 t) {
+    const float2 sn = add2(s, t);
+    const float2 bp = sub2(sn, s);
+    const float2 err = add2(sub2(s, sub2(sn, bp)), sub2(t, bp));
+    s = sn;
+    c = add2(c, err);
+  }
+  __device__ __forceinline__ float2 value() const { return add2(s, c); }
+};
+
+struct PSum2 {
+  float2 s;
+  __device__ __forceinline__ PSum2() : s(make_float2(0.f, 0.f)) {}
+  __device__ __forceinline__ void add(float2 t) { s = add2(s, t); }
+  __device__ __forceinline__ float2 value() const { return s; }
+};
+
 struct PSum {
   float s;
   __device__ __forceinline__ PSum() : s(0.f) {}

@@ -262,10 +262,10 @@ __device__ __forceinline__ uint32_t integrate_and_key(const StepArgs& a, const I
                                                   int cx, int cy, float2 pi, float4 vi, float ax,
                                                   float ay) {
   const float dt = d.dt;
-  float vx = fmaf(dt, ax, vi.x);
-  float vy = fmaf(dt, ay, vi.y);
-  float x = fmaf(dt, vx, pi.x);
-  float y = fmaf(dt, vy, pi.y);
+  const float2 v = fma2(make_float2(dt, dt), make_float2(ax, ay), make_float2(vi.x, vi.y));
+  const float2 xy = fma2(make_float2(dt, dt), v, pi);
+  float vx = v.x, vy = v.y;
+  float x = xy.x, y = xy.y;
   if (d.periodic) {
     if (PREC == 0) {
       if (x >= d.hi_x) x -= d.Lx;

@@ -297,8 +297,8 @@ __device__ __forceinline__ void density_particle(const StepArgs& a, int64_t i) {
           // slot n -- the positions hold one entry more)
           const float2 pn = __ldg(pos + ((kDensityTrim || more ? jn : jj) >> 5));
           const uint32_t j = jj >> 5;
-          float dx = (pi.x - pj.x) - shx;
-          float dy = (pi.y - pj.y) - shy;
+          const float2 dxy = sub2(sub2(pi, pj), make_float2(shx, shy));
+          float dx = dxy.x, dy = dxy.y;
           float r2;
           bool in;
           if (PREC == 0 && (jj & 16u)) {  // plain position reached through the periodic boundary
@@ -714,9 +714,9 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
   const uint32_t key = a.keyA[i];
   const float2 pi = a.posA[i];
   const float4 vi = a.velpA[i];
-  typedef typename std::conditional<PREC == 1, CSum, PSum>::type Sum;
-  // one (compensated) sum per axis of every pair's pressure + viscosity (+ alpha) term
-  Sum fx, fy;
+  // one (compensated) sum per axis of every pair's pressure + viscosity (+ alpha)
+  // term, both axes in paired instructions
+  typename std::conditional<PREC == 1, CSum2, PSum2>::type f;
   const float h = d.h, kp = d.kp, kv = d.kv, tol2 = d.tol2;
   const float alpha_c0 = d.alpha_c0;
   const float rho_i = 1.0f / vi.w;
@@ -728,11 +728,10 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
     const float hr = h - r;
     // viscosity (Laplacian): mu m / (rho_j pi h^6) 45 (h - r) (v_j - v_i); skipped when MU = 0 (the dam
     // breaks' artificial viscosity replaces it), a branch uniform over the instance
-    float tx = 0.f, ty = 0.f;
+    float2 t = make_float2(0.f, 0.f);
     if (!kSkipZeroViscosity || kv != 0.f) {
       const float vm = kv * vj.w * hr;
-      tx = vm * (vj.x - vi.x);
-      ty = vm * (vj.y - vi.y);
+      t = mul2(make_float2(vm, vm), sub2(make_float2(vj.x, vj.y), make_float2(vi.x, vi.y)));
     }
     if (r2 > tol2) {
       // pressure (spiky gradient, symmetric p / rho^2 form)
@@ -747,11 +746,9 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
         }
       }
       s *= hr * hr * rinv;
-      tx = fmaf(s, dx, tx);
-      ty = fmaf(s, dy, ty);
+      t = fma2(make_float2(s, s), make_float2(dx, dy), t);
     }
-    fx.add(tx);
-    fy.add(ty);
+    f.add(t);
   };
   auto pair = [&](uint32_t j, float dx, float dy) { pair_v(__ldg(velp + j), dx, dy); };
   int cx, cy;
@@ -797,9 +794,10 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
       for (int u = 0; u < B; ++u) {
         float dx, dy;
         if (PREC == 1) {  // split: the offsets moved into one cell frame by the tag's stencil offset
-          const float2 o = unit[e[u] & 15u];
-          dx = (pi.x - pj[u].x) - o.x * d.cs_x;
-          dy = (pi.y - pj[u].y) - o.y * d.cs_y;
+          const float2 o = unit[e[u] & 15u];  // (c1, c2) in {-1, 0, 1}: o * cs is exact
+          const float2 dxy = fma2(make_float2(-o.x, -o.y), make_float2(d.cs_x, d.cs_y), sub2(pi, pj[u]));
+          dx = dxy.x;
+          dy = dxy.y;
         } else {
           entry_vec<PREC>(d, pi, pj[u], e[u], dx, dy);
         }
@@ -824,8 +822,8 @@ __device__ __forceinline__ uint32_t force_one(const StepArgs& a, int64_t i, cons
       if (j != (uint32_t)i) pair(j, dx, dy);
     });
   }
-  const float ax = d.gx + fx.value();
-  const float ay = d.gy + fy.value();
+  const float2 acc = add2(make_float2(d.gx, d.gy), f.value());
+  const float ax = acc.x, ay = acc.y;
   if (MODE == kForceOnly) {
     a.acc[i] = make_float2(ax, ay);
     return 0;
