@@ -136,7 +136,9 @@ __device__ __forceinline__ void stencil_keys(const InstDesc& d, uint32_t code, i
                                              uint32_t (&c)[9], uint32_t& valid, uint32_t& wrap) {
   valid = 0;
   wrap = 0;
-  if (!d.periodic && d.order == 0) {
+  // periodic, away from the wrap: the walls' stencil with every cell present
+  const bool inner = d.periodic && cx > 0 && cx + 1 < d.nxr && cy > 0 && cy + 1 < d.nyr;
+  if ((!d.periodic || inner) && d.order == 0) {
     const uint32_t X = code & 0x55555555u, Y = code & 0xAAAAAAAAu;
     const uint32_t xs[3] = {(X - 1u) & 0x55555555u, X, ((X | 0xAAAAAAAAu) + 1u) & 0x55555555u};
     const uint32_t ys[3] = {(Y - 1u) & 0xAAAAAAAAu, Y, ((Y | 0x55555555u) + 1u) & 0xAAAAAAAAu};
@@ -149,7 +151,7 @@ __device__ __forceinline__ void stencil_keys(const InstDesc& d, uint32_t code, i
     }
     return;
   }
-  if (!d.periodic) {  // row-major
+  if (!d.periodic || inner) {  // row-major
     const uint32_t base = d.cell_base + code;
     const bool xo[3] = {cx > 0, true, cx + 1 < d.nx};
     const bool yo[3] = {cy > 0, true, cy + 1 < d.ny};
