@@ -106,6 +106,8 @@ sphg_status make_desc(const sphg_params& p, int64_t begin, int64_t count, uint64
   d.order = p.order;
   d.periodic = p.periodic ? 1 : 0;
   d.active = 1;
+  d.wrap_f32 = (p.periodic && p.lo[0] == 0.0 && p.lo[1] == 0.0 && (double)(float)L[0] == L[0] &&
+                (double)(float)L[1] == L[1]) ? 1 : 0;
   if (p.order == SPHG_ORDER_MORTON) {
     d.nx = next_pow2(nr[0]);
     d.ny = next_pow2(nr[1]);

@@ -29,7 +29,7 @@ struct __align__(16) InstDesc {
   int32_t order;          // 0 Morton, 1 row-major
   int32_t periodic;       // 0 walls, 1 periodic
   int32_t active;         // 0: a finished served instance awaiting compaction (its slots are skipped)
-  int32_t pad_;
+  int32_t wrap_f32;       // periodic, lo = 0, both lengths exact in FP32: minimum images from FP32 operations
   float lo_x, lo_y, hi_x, hi_y;
   float cs_x, cs_y, inv_cs_x, inv_cs_y;
   float Lx, Ly;

@@ -120,8 +120,43 @@ static __device__ __noinline__ bool wrapped_pair_d(float xi, float yi, float xj,
   return true;
 }
 
+// x_i - x_j by the minimum image of one periodic axis of length L (FP32 exact,
+// positions in [0, L)): the FP64 computation's value rounded to FP32, from FP32
+// operations.  Valid when the wrap decision is clear of |d| = L/2 and the
+// operand near 0 is 0 or at least 2^-28 L: the FP64 result is then exact, the
+// operand near L minus L is exact (Sterbenz), and one FP32 operation rounds the
+// exact value.  false: leave it to FP64.
+__device__ __forceinline__ bool min_image_f32(float xi, float xj, float L, float& out) {
+  const float hL = 0.5f * L;
+  const float d0 = xi - xj;  // the exact difference rounded
+  const float ad = fabsf(d0);
+  const float margin = 1.0e-6f * hL;  // > the rounding of d0: the same side of L/2 as the exact difference
+  if (ad < hL - margin) {
+    out = d0;
+    return true;
+  }
+  if (ad <= hL + margin) return false;
+  const bool down = d0 > 0.f;  // x_i near L: d - L; x_j near L: d + L
+  const float near0 = down ? xj : xi, nearL = down ? xi : xj;
+  if (!(near0 >= 0.f) || (near0 != 0.f && near0 < L * 0x1p-28f) || !(nearL >= hL && nearL <= 2.0f * L)) return false;
+  const float t = nearL - L;  // exact
+  out = down ? t - xj : xi - t;
+  return true;
+}
+
 __device__ __forceinline__ bool wrapped_pair(const InstDesc& d, float2 pi, float2 pj, float& dx,
                                              float& dy) {
+  if (d.wrap_f32) {
+    // FP32 minimum images; the FP64 decision only inside the band around h^2
+    float ex, ey;
+    if (min_image_f32(pi.x, pj.x, d.Lx, ex) && min_image_f32(pi.y, pj.y, d.Ly, ey)) {
+      dx = ex;
+      dy = ey;
+      const float r2 = fmaf(ex, ex, ey * ey);
+      if (r2 < d.h2_lo) return true;
+      if (r2 > d.h2_hi) return false;
+    }
+  }
   return wrapped_pair_d(pi.x, pi.y, pj.x, pj.y, d.Lx_d, d.Ly_d, d.half_Lx_d, d.half_Ly_d,
                         d.h2_d, &dx, &dy);
 }
