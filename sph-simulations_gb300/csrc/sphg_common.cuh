@@ -97,10 +97,12 @@ __device__ __forceinline__ int cell_coord(float x, float lo, float inv_cs, doubl
                                           double cs_d, int cmax) {
   float q = (x - lo) * inv_cs;
   if (!(q < (float)cmax + 1.0f)) return cmax;  // also NaN
-  if (q < 0.0f) return 0;
+  float tol = 5.0e-7f * (fabsf(x) + fabsf(lo)) * inv_cs + 1.0e-30f;
+  // clearly below 1 (a particle at or near the low wall): the FP64 quotient is
+  // below 1, its floor 0 or negative, clamped to 0
+  if (q < 1.0f - tol) return 0;
   float fq = floorf(q);
   float fr = q - fq;
-  float tol = 5.0e-7f * (fabsf(x) + fabsf(lo)) * inv_cs + 1.0e-30f;
   int c;
   if (fr > tol && fr < 1.0f - tol) {
     c = (int)fq;

@@ -51,11 +51,15 @@ static __device__ __noinline__ float offset_shift_d(float o, int k, double cs_d)
 }
 
 // floor(o / cs) for a split-precision offset, FP64 near integer boundaries.
+// |q| < 1/2 (an offset at or near the cell's low edge, e.g. a particle resting
+// on a wall) is decided by the sign alone: o / cs lies in (-1, 1), so the FP64
+// floor is 0 for o >= 0 and -1 for o < 0.
 __device__ __forceinline__ int offset_cells(float o, float inv_cs, double cs_d) {
   float q = o * inv_cs;
   float fq = floorf(q);
   float fr = q - fq;
   if (fr > 1.0e-6f && fr < 1.0f - 1.0e-6f && fabsf(q) < 1.0e6f) return (int)fq;
+  if (fabsf(q) < 0.5f) return o < 0.0f ? -1 : 0;
   if (!(fabsf(q) < 1.0e6f)) return 0;  // NaN / runaway: keep the cell; diagnostics flag the state
   return offset_cells_d(o, cs_d);
 }
