@@ -555,6 +555,55 @@ def test_periodic_taylor_green_vs_oracle(prec, order):
     sim.close()
 
 
+@pytest.mark.parametrize("order", ["morton", "rowmajor"])
+@pytest.mark.parametrize("side,h", [(1.0, 0.05), (0.25, 0.08)])
+def test_periodic_minimum_image_at_the_wrap(order, side, h):
+    """Plain positions in a periodic box that starts at 0 and whose side is
+    exact in FP32: pairs reached through the boundary form their minimum image
+    in FP32 (FP64 only near the cut-off, for operands near 0 below 2^-28 of
+    the side, or near a separation of half the side).  Particles placed on
+    both faces, a few ulp from them, at tiny offsets and (in the 3-cell box)
+    near half-side separations: neighbour lists equal the oracle's, densities
+    and forces within the tolerances."""
+    S = _sphg()
+    rng = np.random.default_rng(7)
+    f32 = lambda a: np.asarray(a, np.float64).astype(np.float32).astype(np.float64)  # noqa: E731
+    L = side
+    one_ulp = float(np.spacing(np.float32(L)))
+    edge = [0.0, 2.0 ** -40, 2.0 ** -30, 2.0 ** -27 * L, 3 * 2.0 ** -24, 1e-4 * L,
+            L - one_ulp, L - 3 * one_ulp, L - 1e-4 * L, L - h, h, 0.5 * L, 0.5 * L - one_ulp]
+    pts = set()
+    for ex in edge:
+        for ey in edge:
+            pts.add((ex, ey))
+        for _ in range(3):
+            pts.add((ex, float(rng.uniform(0, L))))
+            pts.add((float(rng.uniform(0, L)), ex))
+    x = np.array([p[0] for p in pts])
+    y = np.array([p[1] for p in pts])
+    x = np.concatenate([x, rng.uniform(0, L, 400)])
+    y = np.concatenate([y, rng.uniform(0, L, 400)])
+    x, y = f32(np.mod(x, L)), f32(np.mod(y, L))
+    keep = (x < L) & (y < L)
+    x, y = x[keep], y[keep]
+    vx, vy = f32(rng.normal(0, 0.1, len(x))), f32(rng.normal(0, 0.1, len(x)))
+    prm = dict(order=order, h=h, dt=1e-5, k=30.0, rho0=1000.0, mu=0.01, gx=0.0, gy=0.0,
+               mass=2e-3 * side * side, alpha=0.0, c0=5.0, lo=(0.0, 0.0), hi=(L, L), periodic=1)
+    p = O.params(**prm)
+    sim = S.Sim(S.params(**prm), len(x), S.options(precision=S.PLAIN))
+    sim.upload(x, y, vx, vy)
+    sim.preloop()
+    a = sim.download()
+    sk, s_, e_, rho, fx, fy = oracle_state(p, a)
+    assert (sim.debug(S.DBG_KEYS) == sk).all()
+    offs, idx = O.neighbor_lists(p, a["x"], a["y"], sk, s_, e_)
+    goffs, gidx = sim.neighbor_lists()
+    assert (goffs == offs).all() and (gidx == idx).all()
+    assert rel_rho(a["rho"], rho) <= RHO_TOL
+    assert rel_acc(a["fx"], a["fy"], fx, fy) <= ACC_TOL
+    sim.close()
+
+
 @pytest.mark.parametrize("prec", ["plain", "split"])
 def test_snapshot_resume_is_exact(prec):
     """sphg_snapshot -> sphg_restore on a fresh handle -> sphg_preloop continues
